@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark: fragments/s of the fill-rate stress frame on one GB300.
+
+Workload (the largest single-GPU configuration of the reference's benchmark
+set that renders one frame): 1920x1080 ARGB8888 colour + f32 depth target,
+100,000 Gouraud triangles given in clip space (screen area log-uniform in
+1..1e4 px^2, ~5% crossing the near/far plane), depth test on, default
+Context.  A step = Frame::clear + one render() of the whole mesh.
+
+value   fragments (Stats.frags.i) per second with the mesh resident in HBM,
+        timed with CUDA events around each step on the library's stream; an
+        L2 flush (512 MiB write) runs between steps, outside the timed span.
+e2e     the same metric through the C ABI with host buffers: per step the
+        mesh is uploaded from pinned host memory (rf_mesh_update), cleared,
+        rendered, and the colour + depth target read back to pinned memory.
+roofline  achieved = algorithmic bytes of the tile rasteriser per frame
+        (4 frags.i + 8 frags.o + 8 W H) / its CUDA-event time; peak = the
+        measured HBM copy bandwidth.
+
+--impl reference times the reference's CPU path (the C++ oracle, a
+restatement of retrofire's render(); Rust is not available here) on the
+host cores, frame-parallel across all of them.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, NTRI, SEED = 1920, 1080, 100_000, 2
+WORKLOAD = "fill_stress_1080p_100k_gouraud"
+METRIC = "frags/s"
+
+
+def config(extra=None):
+    c = {"workload": WORKLOAD, "target": "%dx%d ARGB8888 + f32 depth" % (W, H),
+         "triangles": NTRI, "shader": "gouraud", "seed": SEED,
+         "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas"}
+    c.update(extra or {})
+    return c
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------ CPU side ---
+
+def _oracle_frames(args):
+    """Worker: render `n` frames of the workload with the oracle; returns
+    (seconds, frags_i per frame)."""
+    n, ntri = args
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    from oracle import oracle as O
+    from retrofire_gb300 import scenes
+    s = scenes.fill_stress(ntri=ntri, w=W, h=H, seed=SEED)
+    d = O.make_draw(s["verts"], s["faces"], 1, pos_dim=4)
+    col = np.zeros((H, W), np.uint32)
+    dep = np.zeros((H, W), np.float32)
+    fr = 0
+    t0 = time.perf_counter()
+    for _ in range(n):
+        O.clear(col, dep)
+        st = O.render([d], s["vp"], col, dep, {})
+        fr = st.frags_i
+    return time.perf_counter() - t0, fr
+
+
+def cpu_rate(frames_per_worker, workers):
+    """frags/s of the oracle, `workers` processes (spawned) in parallel."""
+    if workers == 1:
+        t, fr = _oracle_frames((frames_per_worker, NTRI))
+        return fr * frames_per_worker / t, t
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        pool.map(_oracle_frames, [(0, 1000)] * workers)  # import + build warm-up
+        t0 = time.perf_counter()
+        res = pool.map(_oracle_frames, [(frames_per_worker, NTRI)] * workers)
+        wall = time.perf_counter() - t0
+    fr = res[0][1]
+    return fr * frames_per_worker * workers / wall, wall
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as obuild
+    obuild.build()
+    cores = os.cpu_count() or 1
+    times = []
+    _, fr = _oracle_frames((1, NTRI))
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_frames, [(0, 1000)] * cores)
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_oracle_frames, [(1, NTRI)] * cores)
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                times.append(dt)
+    total = sum(times)
+    value = fr * cores * len(times) / total
+    line = {"metric": METRIC, "value": value, "unit": "frags/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": config({"frames_per_step": cores}),
+            "cpu_baseline": {"value": value, "unit": "frags/s", "cores": cores, "kind": "port",
+                             "sample": "%d frames per step, one per core, %d timed steps"
+                                       % (cores, len(times))},
+            "e2e": {"value": value, "unit": "frags/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------ GPU side ---
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the tile rasteriser from the committed ncu
+    summary (profiles/k_raster_fill_1080p.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "k_raster_fill_1080p.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
+    """The metric through the C ABI with pinned host buffers in and out:
+    mesh upload (H2D), clear, render, colour + depth read-back (D2H)."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    pin_v = torch.from_numpy(s["verts"]).pin_memory()
+    pin_i = torch.from_numpy(s["faces"].astype(np.int32)).pin_memory()
+    out_c = torch.empty((H, W), dtype=torch.int32).pin_memory()
+    out_d = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    vnp, inp = pin_v.numpy(), pin_i.numpy().view(np.uint32)
+    cnp, dnp = out_c.numpy().view(np.uint32), out_d.numpy()
+    L = rf.lib()
+
+    def e2e_step():
+        mesh.update(vnp, inp)
+        tg.clear(ctx.color_clear, ctx.depth_clear)
+        st2 = rf.render_draws([(mesh, sh, None)], vp, tg, ctx, sync_stats=True)
+        code = L.rf_target_read(dev.ptr, tg.handle, cnp.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                dnp.ctypes.data_as(C.POINTER(C.c_float)))
+        if code:
+            raise rf.RfError(code, "rf_target_read")
+        return st2
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    lat = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st2 = e2e_step()
+        lat.append(time.perf_counter() - t0)
+    assert st2.frags_i == frags_i
+    lat_ms = sorted(x * 1e3 for x in lat)
+    return {"value": frags_i * args.steps * world / sum(lat), "unit": "frags/s",
+            "h2d_bytes_per_step": int(s["verts"].nbytes + s["faces"].nbytes),
+            "d2h_bytes_per_step": int(2 * 4 * W * H),
+            "latency_ms": {"p50": lat_ms[len(lat_ms) // 2],
+                           "p99": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))]}}
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import scenes
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        # Single-threaded oracle on a bounded sample (the reference renders
+        # on one thread), measured before the GPU work starts.
+        r1, t1 = cpu_rate(args.cpu_frames, 1)
+        cpu = {"value": r1, "unit": "frags/s", "cores": 1, "kind": "port",
+               "sample": "%d full frames of the workload, single thread, %.1f s"
+                         % (args.cpu_frames, t1)}
+
+    s = scenes.fill_stress(ntri=NTRI, w=W, h=H, seed=SEED)
+    stream = torch.cuda.Stream()
+    dev = rf.Device(stream.cuda_stream)
+    if args.tile or args.warps:
+        dev.set_tiling(args.tile, args.warps)
+    mesh = rf.Mesh(s["verts"], s["faces"], pos_dim=4, device=dev)
+    tg = rf.Framebuf(W, H, rf.ARGB8888, True, device=dev)
+    sh = rf.Shader.gouraud()
+    ctx = rf.Context()
+    vp = s["vp"]
+    flush = None if args.no_flush else torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step(sync_stats=False):
+        tg.clear(ctx.color_clear, ctx.depth_clear)
+        return rf.render_draws([(mesh, sh, None)], vp, tg, ctx, sync_stats=sync_stats)
+
+    st = step(sync_stats=True)  # one frame for the per-frame stats
+    frags_i, frags_o = st.frags_i, st.frags_o
+    for _ in range(args.warmup):
+        step()
+    dev.sync()
+    dev.stage_ms()  # discard warm-up timings
+    dev.set_timing(True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            if flush is not None:
+                flush.fill_(i & 0xFF)
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    stage, nfr = dev.stage_ms()
+    dev.set_timing(False)
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / args.steps
+    value = frags_i * args.steps * world / (total_ms / 1e3)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world)
+
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        raster_ms = stage["raster"] / max(nfr, 1)
+        alg_bytes = 4 * frags_i + 8 * frags_o + 8 * W * H
+        achieved = alg_bytes / (raster_ms / 1e3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": "frags/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded fill-rate stress scene)",
+            "config": config({"tile_w": args.tile or 32, "warps_per_block": args.warps or 4}),
+            "tris_per_s": NTRI * args.steps * world / (total_ms / 1e3),
+            "frames_per_s": args.steps * world / (total_ms / 1e3),
+            "frags_o_per_frame": frags_o, "frags_i_per_frame": frags_i,
+            "stage_ms_per_frame": {k: v / max(nfr, 1) for k, v in stage.items()},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": ncu_traffic(),
+                         "kernel": "k_raster", "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 7 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    for o in (mesh, tg):
+        o.close()
+    dev.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--cpu-frames", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
+    ap.add_argument("--no-flush", action="store_true", help="no L2 flush buffer (profiling)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import __graft_entry__
+    __graft_entry__.build()
+    run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * rfgpu.h — C ABI of the GB300 (sm_103a) triangle rendering library.
+ *
+ * Drop-in boundary for retrofire's rendering hot path.  The reference entry
+ * point is the generic Rust function
+ *
+ *   pub fn render(prims, verts, shader: &Shd, uniform: Uni,
+ *                 to_screen: Mat4<Ndc, Screen>, target: &mut impl Target,
+ *                 ctx: &Context)                    core/src/render.rs:134-147
+ *
+ * which transforms vertices, clips against the view frustum, maps to the
+ * viewport, culls, scan-converts and depth-tests into a Buf2 colour/depth
+ * target on the CPU.  Here the same path runs as CUDA kernels on one GPU;
+ * meshes, textures and targets are device-resident objects named by handle.
+ * Results (coverage, depth, stats) are bit-identical to the reference; colour
+ * is bit-identical except for RF_SHADER_GOURAUD_SRGB (powf, +-1 LSB).
+ *
+ * Threading: one rf_ctx per host thread; each rf_ctx is bound to one CUDA
+ * stream and every call on it is ordered on that stream.  Nothing here traps
+ * or panics on the device: out-of-range input is reported by status code or
+ * counted in rf_stats.oob (the reference panics on those, buf.rs:444-449).
+ */
+#ifndef RFGPU_H
+#define RFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t rf_status;
+#define RF_OK 0
+#define RF_ERR_BAD_HANDLE 1
+#define RF_ERR_BAD_ARG 2
+#define RF_ERR_NON_POT_TEXTURE 3 /* SamplerRepeatPot::new panics (tex.rs:227-233) */
+#define RF_ERR_OOM 4
+#define RF_ERR_OVER_BUDGET 5
+#define RF_ERR_OVERFLOW 6
+#define RF_ERR_TIMEOUT 7
+#define RF_ERR_CUDA 8
+#define RF_ERR_NO_DEVICE 9
+
+typedef struct rf_ctx rf_ctx;
+typedef uint64_t rf_mesh;
+typedef uint64_t rf_texture;
+typedef uint64_t rf_target;
+
+/* Fixed shader family replacing the reference's closure shaders
+ * (core/src/render/shader.rs:31-76).  Vertex side of every kind:
+ * `vertex(mvp.apply(&v.pos), v.attrib)` (mat.rs:952-973), or the clip-space
+ * passthrough `vertex(v.pos, v.attrib)` for meshes uploaded with pos_dim 4. */
+enum {
+    RF_SHADER_FLAT = 0,         /* attrib (): constant Color4 (benches/fill.rs:21-34) */
+    RF_SHADER_GOURAUD = 1,      /* attrib Color3f: frag.var.to_color4() (color.rs:253-263) */
+    RF_SHADER_TEXTURED = 2,     /* attrib TexCoord: sampler.sample(&tex, frag.var) (tex.rs) */
+    RF_SHADER_TEX_GOURAUD = 3,  /* attrib (Color3f, TexCoord):
+                                   (texel.to_rgb().to_color3f() * col).to_color4() */
+    RF_SHADER_GOURAUD_SRGB = 4  /* attrib linear Color3f: frag.var.to_srgb().to_color4()
+                                   (core/examples/hello_tri.rs:12-20) */
+};
+enum { RF_SAMPLER_REPEAT_POT = 0, RF_SAMPLER_CLAMP = 1, RF_SAMPLER_ONCE = 2 };
+/* u32 colour formats, IntoPixel<u32, F> (util/pixfmt.rs:76-103). */
+enum { RF_ARGB8888 = 0, RF_XRGB8888 = 1, RF_RGBA8888 = 2, RF_BGRA8888 = 3 };
+/* Context::depth_test (ctx.rs:41-47): None, Some(Less), Some(Equal), Some(Greater). */
+enum { RF_DEPTH_NONE = 0, RF_DEPTH_LESS = 1, RF_DEPTH_EQUAL = 2, RF_DEPTH_GREATER = 3 };
+/* Context::face_cull (ctx.rs:21-27). */
+enum { RF_CULL_NONE = 0, RF_CULL_BACK = 1, RF_CULL_FRONT = 2 };
+
+/* The `uniform` argument of render() for the fixed shader family. */
+typedef struct {
+    float mvp[16];        /* ProjMat3<Model>, row-major like Matrix.0 (mat.rs:77-80) */
+    uint32_t flat_rgba;   /* RF_SHADER_FLAT: Color4 bytes r,g,b,a, little-endian */
+    uint32_t sampler;     /* RF_SAMPLER_* */
+    rf_texture texture;   /* RF_SHADER_TEXTURED / RF_SHADER_TEX_GOURAUD */
+} rf_uniforms;
+
+/* Context (ctx.rs:11-65) without the clears (rf_target_clear) and stats
+ * (returned in rf_stats).  Context::default() == {LESS, 1, 1, BACK}.
+ * depth_sort is not supported: the reference sorts with sort_unstable_by,
+ * whose order of equal keys is unspecified. */
+typedef struct {
+    int32_t depth_test;
+    int32_t color_write;
+    int32_t depth_write;
+    int32_t face_cull;
+} rf_context_flags;
+
+/* Stats / Throughput (render/stats.rs:16-40).  oob counts scanlines that
+ * left the target buffer (where the reference would panic). */
+typedef struct {
+    uint64_t calls, prims_i, prims_o, verts_i, verts_o, frags_i, frags_o, oob;
+} rf_stats;
+
+/* One render() call for rf_render_draws (Batch::render, batch.rs:127-146). */
+typedef struct {
+    rf_mesh mesh;
+    int32_t shader;
+    int32_t pad_;
+    rf_uniforms uniforms;
+} rf_draw;
+
+/* ---- context ---------------------------------------------------------- */
+/* cuda_stream: a cudaStream_t to run on, or NULL for a new private stream.
+ * Replaces the reference's implicit single thread (render.rs:134). */
+rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out);
+rf_status rf_ctx_destroy(rf_ctx *ctx);
+/* Waits for all work queued on the context's stream. */
+rf_status rf_ctx_sync(rf_ctx *ctx);
+/* Adds the stats of every render since the last call into *out (and syncs). */
+rf_status rf_ctx_take_stats(rf_ctx *ctx, rf_stats *out);
+const char *rf_status_str(rf_status s);
+/* Tile raster tuning: tile width in pixels (8, 16, 32 or 64; tiles are 32
+ * rows high) and rasteriser warps per block.  0 keeps the current value. */
+rf_status rf_ctx_set_tiling(rf_ctx *ctx, uint32_t tile_w, uint32_t warps_per_block);
+
+/* Per-stage GPU timing (the device side of Stats::time, stats.rs:57-78).
+ * When enabled, every render records CUDA events around its stages on the
+ * context's stream; rf_ctx_stage_ms waits for the stream, adds the elapsed
+ * milliseconds of every timed render since the last call into
+ * out[0..RF_STAGE_N) and returns the number of renders timed in *frames. */
+#define RF_STAGE_VERTEX 0
+#define RF_STAGE_CLIP 1
+#define RF_STAGE_SCAN 2
+#define RF_STAGE_SETUP 3
+#define RF_STAGE_RASTER 4
+#define RF_STAGE_N 5
+rf_status rf_ctx_set_timing(rf_ctx *ctx, int32_t enable);
+rf_status rf_ctx_stage_ms(rf_ctx *ctx, double out[RF_STAGE_N], uint32_t *frames);
+
+/* ---- resources (replace borrowed slices / Buf2s, render.rs:149-150) ---- */
+/* verts: nverts * (pos_dim + nattr) floats, pos_dim 3 (Vertex3) or 4 (clip
+ * space); idx: ntri * 3 u32 (Tri<usize>, geom/prim.rs:33). */
+rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
+                         uint32_t nattr, const uint32_t *idx, uint32_t ntri, rf_mesh *out);
+/* Replaces the contents of a mesh with arrays of the same sizes (an
+ * animated or re-submitted mesh without reallocation). */
+rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx);
+rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh);
+/* rgba: w*h texels, Color4 bytes r,g,b,a little-endian, row-major
+ * (Texture<Buf2<Color4>>, tex.rs:33-37). */
+rf_status rf_texture_upload(rf_ctx *ctx, const uint32_t *rgba, uint32_t w, uint32_t h,
+                            rf_texture *out);
+rf_status rf_texture_destroy(rf_ctx *ctx, rf_texture tex);
+/* Framebuf<Colorbuf<Buf2<u32>, pixfmt>, Buf2<f32>> (target.rs:35-44) when
+ * has_depth, else a colour-only Colorbuf (target.rs:138-161).  Contents
+ * start zeroed, like Buf2::new (buf.rs:155-161). */
+rf_status rf_target_create(rf_ctx *ctx, uint32_t w, uint32_t h, int32_t pixfmt,
+                           int32_t has_depth, rf_target *out);
+rf_status rf_target_destroy(rf_ctx *ctx, rf_target t);
+/* Frame::clear (front/src/lib.rs:103-120): colour <- into_pixel(*clear_rgba),
+ * depth <- 1 / *depth_clear; NULL leaves that buffer alone.  The fill is
+ * fused into the next render's tile loads. */
+rf_status rf_target_clear(rf_ctx *ctx, rf_target t, const uint32_t *clear_rgba,
+                          const float *depth_clear);
+rf_status rf_target_write(rf_ctx *ctx, rf_target t, const uint32_t *color, const float *depth);
+/* Copies the target to host memory (synchronous); NULL skips a buffer. */
+rf_status rf_target_read(rf_ctx *ctx, rf_target t, uint32_t *color, float *depth);
+
+/* ---- rendering -------------------------------------------------------- */
+/* render(mesh.faces, mesh.verts, shader, uniforms, viewport, target, ctx)
+ * (render.rs:134-207).  viewport: Mat4<Ndc, Screen>, row-major.  When stats
+ * is non-NULL the call waits for completion and stores this call's stats
+ * (like `*ctx.stats.borrow_mut() += stats`, render.rs:206); with NULL it
+ * only queues the work and the stats accumulate for rf_ctx_take_stats. */
+rf_status rf_render(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_uniforms *uniforms,
+                    const float viewport[16], rf_target target, const rf_context_flags *flags,
+                    rf_stats *stats);
+/* ndraws consecutive render() calls into one target, in order, as one GPU
+ * pass (the per-object submission idiom of demos/src/bin/crates.rs:114-133).
+ * The result equals calling rf_render once per draw in order. */
+rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
+                          const float viewport[16], rf_target target,
+                          const rf_context_flags *flags, rf_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -240,9 +240,18 @@ struct Scanline {
     uint32_t count;      // vary(..., Some(count))
 };
 
+// Scanline origins beyond +-2^22 px are outside the supported domain (the
+// row arithmetic y0r + j stops being exact); such a half is skipped and
+// reported through `oob` instead of being walked.
+constexpr float MAX_COORD = 4194304.0f;
+
 // raster.rs:80-114 + vary.rs:142-155: emits every scanline of one half.
-template <int NA, class F>
-void run_scan(ScanIter<NA> it, F &&f) {
+template <int NA, class F, class G>
+void run_scan(ScanIter<NA> it, F &&f, G &&oob) {
+    if (it.n != 0 && !(std::fabs(it.y) < MAX_COORD)) {
+        oob();
+        return;
+    }
     while (it.n != 0) {
         Var<NA> v0 = it.left;                 // left.next(): current value ...
         it.left = vstep(it.left, it.dl);      // ... then step
@@ -264,8 +273,8 @@ void run_scan(ScanIter<NA> it, F &&f) {
 }
 
 // raster.rs:185-224 tri_fill.
-template <int NA, class F>
-void tri_fill(const Var<NA> verts_in[3], F &&f) {
+template <int NA, class F, class G>
+void tri_fill(const Var<NA> verts_in[3], F &&f, G &&oob) {
     // Stable sort by y with total_cmp (slice::sort_by is stable).
     Var<NA> v[3] = {verts_in[0], verts_in[1], verts_in[2]};
     for (int i = 1; i < 3; ++i)
@@ -279,8 +288,8 @@ void tri_fill(const Var<NA> verts_in[3], F &&f) {
     Var<NA> mid1 = vlerp(top, bot, (mid_y - top_y) / (bot_y - top_y));
     const Var<NA> &left = (mid0.p[0] < mid1.p[0]) ? mid0 : mid1;
     const Var<NA> &right = (mid0.p[0] < mid1.p[0]) ? mid1 : mid0;
-    run_scan<NA>(scan<NA>(top_y, mid_y, top, left, top, right), f);
-    run_scan<NA>(scan<NA>(mid_y, bot_y, left, bot, right, bot), f);
+    run_scan<NA>(scan<NA>(top_y, mid_y, top, left, top, right), f, oob);
+    run_scan<NA>(scan<NA>(mid_y, bot_y, left, bot, right, bot), f, oob);
 }
 
 // ------------------------------------------------------------ shading ---
@@ -424,15 +433,18 @@ void render_t(const rfo_draw *d, const float vp[16], uint32_t *color, float *dep
             st->verts_o += 3;
 
             tri_fill<NA>(sv, [&](const Scanline<NA> &sl) {
+                // The reference panics when a scanline leaves the buffer
+                // (buf.rs slice indexing).  Here a row below the buffer only
+                // counts in oob; a span past the right edge counts in oob,
+                // keeps its frags.i and drops the pixels past the edge.
+                if (sl.y >= h) {
+                    st->oob += 1;
+                    return;
+                }
                 uint64_t x0 = sl.x0;
                 uint64_t x1 = sl.x1 > x0 ? sl.x1 : x0;
                 st->frags_i += x1 - x0;
-                // The reference panics when the span leaves the buffer
-                // (buf.rs slice indexing); here the row or the excess is
-                // dropped and counted.
-                bool bad = sl.y >= h || x1 > w;
-                if (bad) st->oob += 1;
-                if (sl.y >= h) return;
+                if (x1 > w) st->oob += 1;
                 uint64_t nfr = x1 - x0;
                 if (sl.count < nfr) nfr = sl.count;  // zip() truncation
                 Var<NA> v = sl.v0;
@@ -466,7 +478,7 @@ void render_t(const rfo_draw *d, const float vp[16], uint32_t *color, float *dep
                     }
                     v = vstep(v, sl.dv_dx);  // Iter::next, vary.rs:146-154
                 }
-            });
+            }, [&] { st->oob += 1; });
         }
     }
     delete[] cv;
@@ -556,7 +568,7 @@ uint32_t tri_fill_test(const float *screen, const float *attr, uint32_t zmask, u
             ++nf;
             q = vstep(q, sl.dv_dx);
         }
-    });
+    }, [] {});
     *nfrags = nf;
     return nr;
 }

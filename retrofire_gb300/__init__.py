@@ -1,0 +1,400 @@
+"""retrofire_gb300 — retrofire's triangle render path on a GB300 (sm_103a).
+
+Python host mirror of the reference's rendering surface over the C ABI of
+librfgpu (include/rfgpu.h):
+
+    render(prims, verts, shader, uniform, to_screen, target, ctx)
+        core/src/render.rs:134-207
+    Context                      core/src/render/ctx.rs:11-126
+    Framebuf / Colorbuf          core/src/render/target.rs:35-44
+    shader kinds                 core/src/render/shader.rs (fixed family)
+    Texture + samplers           core/src/render/tex.rs
+    Stats                        core/src/render/stats.rs:16-40
+
+Meshes, textures and targets live on the device; ``render`` uploads the
+given vertex/index arrays (a fresh mesh per call, like the reference's
+borrowed slices) unless a ``Mesh`` handle is passed.  There is no CPU
+fallback: without the CUDA library every entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import mat  # noqa: F401  (host-side matrix helpers)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "librfgpu.so")
+
+# Shader kinds, samplers, pixel formats, depth tests, face culling
+# (mirrors of include/rfgpu.h).
+FLAT, GOURAUD, TEXTURED, TEX_GOURAUD, GOURAUD_SRGB = range(5)
+REPEAT_POT, CLAMP, ONCE = range(3)
+ARGB8888, XRGB8888, RGBA8888, BGRA8888 = range(4)
+DEPTH_NONE, DEPTH_LESS, DEPTH_EQUAL, DEPTH_GREATER = range(4)
+CULL_NONE, CULL_BACK, CULL_FRONT = range(3)
+NATTR = {FLAT: 0, GOURAUD: 3, TEXTURED: 2, TEX_GOURAUD: 5, GOURAUD_SRGB: 3}
+
+STAGES = ("vertex", "clip", "scan", "setup", "raster")
+
+STATUS = {0: "ok", 1: "bad handle", 2: "bad argument", 3: "non power-of-two texture",
+          4: "out of device memory", 5: "over budget", 6: "overflow", 7: "timeout",
+          8: "cuda error", 9: "no cuda device"}
+
+
+class RfError(RuntimeError):
+    def __init__(self, code, what=""):
+        super().__init__("%s: %s (%d)" % (what, STATUS.get(code, "?"), code))
+        self.code = code
+
+
+class Uniforms(C.Structure):
+    _fields_ = [("mvp", C.c_float * 16), ("flat_rgba", C.c_uint32), ("sampler", C.c_uint32),
+                ("texture", C.c_uint64)]
+
+
+class Flags(C.Structure):
+    _fields_ = [("depth_test", C.c_int32), ("color_write", C.c_int32),
+                ("depth_write", C.c_int32), ("face_cull", C.c_int32)]
+
+
+class CStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("calls", "prims_i", "prims_o", "verts_i", "verts_o",
+                                          "frags_i", "frags_o", "oob")]
+
+
+class Draw(C.Structure):
+    _fields_ = [("mesh", C.c_uint64), ("shader", C.c_int32), ("pad_", C.c_int32),
+                ("uniforms", Uniforms)]
+
+
+# Exported symbols of include/rfgpu.h with their ctypes signatures.
+_P = C.c_void_p
+_SIGS = {
+    "rf_ctx_create": [_P, C.POINTER(_P)],
+    "rf_ctx_destroy": [_P],
+    "rf_ctx_sync": [_P],
+    "rf_ctx_take_stats": [_P, C.POINTER(CStats)],
+    "rf_ctx_set_tiling": [_P, C.c_uint32, C.c_uint32],
+    "rf_mesh_upload": [_P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_uint32,
+                       C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint64)],
+    "rf_mesh_update": [_P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_uint32)],
+    "rf_mesh_destroy": [_P, C.c_uint64],
+    "rf_ctx_set_timing": [_P, C.c_int32],
+    "rf_ctx_stage_ms": [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
+    "rf_texture_upload": [_P, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32,
+                          C.POINTER(C.c_uint64)],
+    "rf_texture_destroy": [_P, C.c_uint64],
+    "rf_target_create": [_P, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32,
+                         C.POINTER(C.c_uint64)],
+    "rf_target_destroy": [_P, C.c_uint64],
+    "rf_target_clear": [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_float)],
+    "rf_target_write": [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_float)],
+    "rf_target_read": [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_float)],
+    "rf_render": [_P, C.c_uint64, C.c_int32, C.POINTER(Uniforms), C.POINTER(C.c_float),
+                  C.c_uint64, C.POINTER(Flags), C.POINTER(CStats)],
+    "rf_render_draws": [_P, C.POINTER(Draw), C.c_uint32, C.POINTER(C.c_float), C.c_uint64,
+                        C.POINTER(Flags), C.POINTER(CStats)],
+}
+
+_lib = None
+
+
+def lib():
+    """Load librfgpu.so (built by retrofire_gb300.build); raise if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("librfgpu.so is not built (%s); run "
+                               "`python -m retrofire_gb300.build`" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, argt in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = argt
+            fn.restype = C.c_int32
+        L.rf_status_str.argtypes = [C.c_int32]
+        L.rf_status_str.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(code, what):
+    if code != 0:
+        raise RfError(code, what)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _u32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+class Stats:
+    """Stats (stats.rs:16-40): calls and per-stage Throughput in/out."""
+    FIELDS = ("calls", "prims_i", "prims_o", "verts_i", "verts_o", "frags_i", "frags_o", "oob")
+
+    def __init__(self, **kw):
+        for f in self.FIELDS:
+            setattr(self, f, int(kw.get(f, 0)))
+
+    @classmethod
+    def from_c(cls, cs):
+        return cls(**{f: getattr(cs, f) for f in cls.FIELDS})
+
+    def __iadd__(self, o):
+        for f in self.FIELDS:
+            setattr(self, f, getattr(self, f) + getattr(o, f))
+        return self
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f in self.FIELDS}
+
+    def __repr__(self):
+        return "Stats(%s)" % ", ".join("%s=%d" % kv for kv in self.as_dict().items())
+
+
+class Context:
+    """Context (ctx.rs:11-126); defaults equal Context::default()."""
+
+    def __init__(self, color_clear=0xFF000000, depth_clear=float("inf"), face_cull=CULL_BACK,
+                 depth_test=DEPTH_LESS, color_write=True, depth_write=True, depth_sort=None):
+        if depth_sort is not None:
+            raise NotImplementedError("depth_sort: the reference's unstable sort has no "
+                                      "defined order for equal depths")
+        self.color_clear = color_clear    # Color4 as r|g<<8|b<<16|a<<24, or None
+        self.depth_clear = depth_clear    # f32 or None
+        self.face_cull = face_cull
+        self.depth_test = depth_test
+        self.color_write = color_write
+        self.depth_write = depth_write
+        self.stats = Stats()
+
+    def flags(self):
+        return Flags(self.depth_test, int(bool(self.color_write)), int(bool(self.depth_write)),
+                     self.face_cull)
+
+
+class Device:
+    """One rf_ctx: a CUDA stream plus the handles created on it."""
+
+    def __init__(self, stream=None):
+        p = _P()
+        _check(lib().rf_ctx_create(stream, C.byref(p)), "rf_ctx_create")
+        self.ptr = p
+
+    def close(self):
+        if self.ptr:
+            lib().rf_ctx_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        _check(lib().rf_ctx_sync(self.ptr), "rf_ctx_sync")
+
+    def set_tiling(self, tile_w=0, warps=0):
+        _check(lib().rf_ctx_set_tiling(self.ptr, tile_w, warps), "rf_ctx_set_tiling")
+
+    def set_timing(self, enable=True):
+        _check(lib().rf_ctx_set_timing(self.ptr, int(bool(enable))), "rf_ctx_set_timing")
+
+    def stage_ms(self):
+        """Per-stage GPU milliseconds summed over the timed renders since the
+        last call, and the number of renders: ({stage: ms}, frames)."""
+        out = (C.c_double * 5)()
+        fr = C.c_uint32()
+        _check(lib().rf_ctx_stage_ms(self.ptr, out, C.byref(fr)), "rf_ctx_stage_ms")
+        return dict(zip(STAGES, list(out))), fr.value
+
+    def take_stats(self):
+        cs = CStats()
+        _check(lib().rf_ctx_take_stats(self.ptr, C.byref(cs)), "rf_ctx_take_stats")
+        return Stats.from_c(cs)
+
+
+_default_device = None
+
+
+def default_device():
+    global _default_device
+    if _default_device is None:
+        _default_device = Device()
+    return _default_device
+
+
+class Mesh:
+    """Device-resident Mesh (geom/mesh.rs:24-30): vertex array + Tri<usize> faces.
+
+    verts: (n, pos_dim + nattr) float32, pos_dim 3 (model space) or 4 (clip
+    space, passed through the vertex shader unchanged)."""
+
+    def __init__(self, verts, faces, pos_dim=3, device=None):
+        self.dev = device or default_device()
+        v = np.ascontiguousarray(verts, np.float32)
+        f = np.ascontiguousarray(faces, np.uint32).reshape(-1)
+        if v.ndim != 2 or v.shape[1] < pos_dim:
+            raise ValueError("verts must be (n, pos_dim + nattr)")
+        self.nverts, self.ntri = v.shape[0], f.size // 3
+        self.pos_dim, self.nattr = pos_dim, v.shape[1] - pos_dim
+        h = C.c_uint64()
+        _check(lib().rf_mesh_upload(self.dev.ptr, _fp(v), v.shape[0], pos_dim, self.nattr,
+                                    _u32p(f), self.ntri, C.byref(h)), "rf_mesh_upload")
+        self.handle = h.value
+
+    def update(self, verts=None, faces=None):
+        """rf_mesh_update: same-sized arrays, uploaded in place."""
+        v = None if verts is None else np.ascontiguousarray(verts, np.float32)
+        f = None if faces is None else np.ascontiguousarray(faces, np.uint32)
+        _check(lib().rf_mesh_update(self.dev.ptr, self.handle, _fp(v) if v is not None else None,
+                                    _u32p(f) if f is not None else None), "rf_mesh_update")
+
+    def close(self):
+        if self.handle and self.dev.ptr:
+            lib().rf_mesh_destroy(self.dev.ptr, self.handle)
+        self.handle = 0
+
+
+class Texture:
+    """Texture<Buf2<Color4>> (tex.rs:33-37); texels (h, w) u32 = bytes r,g,b,a."""
+
+    def __init__(self, texels, device=None):
+        self.dev = device or default_device()
+        t = np.ascontiguousarray(texels, np.uint32)
+        self.h, self.w = t.shape
+        h = C.c_uint64()
+        _check(lib().rf_texture_upload(self.dev.ptr, _u32p(t), self.w, self.h, C.byref(h)),
+               "rf_texture_upload")
+        self.handle = h.value
+
+    def close(self):
+        if self.handle and self.dev.ptr:
+            lib().rf_texture_destroy(self.dev.ptr, self.handle)
+        self.handle = 0
+
+
+class Framebuf:
+    """Framebuf<Colorbuf<Buf2<u32>, fmt>, Buf2<f32>> (target.rs:35-44) on the
+    device; with depth=False a colour-only Colorbuf (target.rs:187-202)."""
+
+    def __init__(self, w, h, pixfmt=ARGB8888, depth=True, device=None):
+        self.dev = device or default_device()
+        self.w, self.h, self.pixfmt, self.has_depth = w, h, pixfmt, depth
+        hd = C.c_uint64()
+        _check(lib().rf_target_create(self.dev.ptr, w, h, pixfmt, int(depth), C.byref(hd)),
+               "rf_target_create")
+        self.handle = hd.value
+
+    def clear(self, color_clear=0xFF000000, depth_clear=float("inf")):
+        """Frame::clear (front/src/lib.rs:103-120); None skips a buffer."""
+        cc = (C.c_uint32 * 1)(color_clear) if color_clear is not None else None
+        dc = (C.c_float * 1)(depth_clear) if depth_clear is not None else None
+        _check(lib().rf_target_clear(self.dev.ptr, self.handle,
+                                     C.cast(cc, C.POINTER(C.c_uint32)) if cc else None,
+                                     C.cast(dc, C.POINTER(C.c_float)) if dc else None),
+               "rf_target_clear")
+
+    def write(self, color=None, depth=None):
+        c = None if color is None else np.ascontiguousarray(color, np.uint32)
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+        _check(lib().rf_target_write(self.dev.ptr, self.handle, _u32p(c) if c is not None else None,
+                                     _fp(d) if d is not None else None), "rf_target_write")
+
+    def read(self):
+        color = np.empty((self.h, self.w), np.uint32)
+        depth = np.empty((self.h, self.w), np.float32) if self.has_depth else None
+        _check(lib().rf_target_read(self.dev.ptr, self.handle, _u32p(color),
+                                    _fp(depth) if depth is not None else None), "rf_target_read")
+        return color, depth
+
+    def close(self):
+        if self.handle and self.dev.ptr:
+            lib().rf_target_destroy(self.dev.ptr, self.handle)
+        self.handle = 0
+
+
+class Shader:
+    """A member of the fixed shader family with its non-matrix uniforms."""
+
+    def __init__(self, kind, flat_rgba=0, texture=None, sampler=REPEAT_POT):
+        self.kind, self.flat_rgba, self.texture, self.sampler = kind, flat_rgba, texture, sampler
+
+    @classmethod
+    def flat(cls, rgba):
+        return cls(FLAT, flat_rgba=rgba)
+
+    @classmethod
+    def gouraud(cls):
+        return cls(GOURAUD)
+
+    @classmethod
+    def gouraud_srgb(cls):
+        return cls(GOURAUD_SRGB)
+
+    @classmethod
+    def textured(cls, texture, sampler=REPEAT_POT):
+        return cls(TEXTURED, texture=texture, sampler=sampler)
+
+    @classmethod
+    def tex_gouraud(cls, texture, sampler=REPEAT_POT):
+        return cls(TEX_GOURAUD, texture=texture, sampler=sampler)
+
+    def uniforms(self, mvp):
+        u = Uniforms()
+        m = np.eye(4, dtype=np.float32) if mvp is None else np.asarray(mvp, np.float32)
+        u.mvp[:] = [float(x) for x in m.reshape(-1)]
+        u.flat_rgba = self.flat_rgba
+        u.sampler = self.sampler
+        u.texture = self.texture.handle if self.texture is not None else 0
+        return u
+
+
+def render(prims, verts, shader, uniform, to_screen, target, ctx=None, pos_dim=3):
+    """render() (render.rs:134-207).
+
+    prims: Mesh, or (n, 3) vertex indices with verts (n, pos_dim + nattr);
+    uniform: the 4x4 mvp (ProjMat3); to_screen: the 4x4 viewport matrix;
+    target: Framebuf; ctx: Context (stats are added into ctx.stats)."""
+    ctx = ctx or Context()
+    dev = target.dev
+    own = not isinstance(prims, Mesh)
+    mesh = Mesh(verts, prims, pos_dim=pos_dim, device=dev) if own else prims
+    try:
+        vp = np.ascontiguousarray(to_screen, np.float32).reshape(-1)
+        u = shader.uniforms(uniform)
+        fl = ctx.flags()
+        cs = CStats()
+        _check(lib().rf_render(dev.ptr, mesh.handle, shader.kind, C.byref(u), _fp(vp),
+                               target.handle, C.byref(fl), C.byref(cs)), "rf_render")
+        st = Stats.from_c(cs)
+        ctx.stats += st
+        return st
+    finally:
+        if own:
+            mesh.close()
+
+
+def render_draws(draws, to_screen, target, ctx=None, sync_stats=True):
+    """Several render() calls into one target, in order, as one GPU pass.
+
+    draws: list of (Mesh, Shader, mvp)."""
+    ctx = ctx or Context()
+    arr = (Draw * len(draws))()
+    for i, (mesh, shader, mvp) in enumerate(draws):
+        arr[i].mesh = mesh.handle
+        arr[i].shader = shader.kind
+        arr[i].uniforms = shader.uniforms(mvp)
+    vp = np.ascontiguousarray(to_screen, np.float32).reshape(-1)
+    fl = ctx.flags()
+    cs = CStats()
+    _check(lib().rf_render_draws(target.dev.ptr, arr, len(draws), _fp(vp), target.handle,
+                                 C.byref(fl), C.byref(cs) if sync_stats else None),
+           "rf_render_draws")
+    st = Stats.from_c(cs)
+    ctx.stats += st
+    return st

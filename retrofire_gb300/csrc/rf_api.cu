@@ -1,0 +1,629 @@
+// rf_api.cu — the C ABI of include/rfgpu.h: handle tables, device arenas and
+// the per-frame launch sequence of the render path.
+//
+// A frame = one or more "jobs" (a target plus its draws).  rf_render and
+// rf_render_draws build one job; every draw is one reference render() call
+// (core/src/render.rs:134-207) and the draws of a job are rendered in order.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/rfgpu.h"
+#include "rf_internal.cuh"
+#include "rf_kernels.cuh"
+
+namespace {
+
+struct Mesh {
+    float *verts = nullptr;
+    uint32_t *idx = nullptr;
+    uint32_t nverts = 0, ntri = 0, pos_dim = 3, nattr = 0;
+};
+struct Texture {
+    uint32_t *texels = nullptr;
+    uint32_t w = 0, h = 0;
+};
+struct Target {
+    uint32_t *color = nullptr;
+    float *depth = nullptr;
+    uint32_t w = 0, h = 0;
+    int32_t fmt = RF_ARGB8888;
+    uint32_t clear_flags = 0;  // pending Frame::clear, fused into the next render
+    uint32_t clear_px = 0;
+    float clear_z = 0.0f;
+};
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+}  // namespace
+
+struct rf_ctx {
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int nsm = 1;
+    uint32_t tile_w = 32, warps = 4;
+    uint64_t next_handle = 1;
+    std::unordered_map<uint64_t, Mesh> meshes;
+    std::unordered_map<uint64_t, Texture> textures;
+    std::unordered_map<uint64_t, Target> targets;
+    // per-frame scratch
+    DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
+    // stats: host-side counts + device-accumulated counts, and what was
+    // already handed out by rf_ctx_take_stats / rf_render
+    rf_stats host_acc{};
+    rf_stats taken{};
+    char last_error[256] = {0};
+    std::vector<DrawDev> hdraws;
+    std::vector<JobDev> hjobs;
+    // stage timing
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<std::vector<cudaEvent_t>> ev_pending;  // RF_STAGE_N + 1 events per render
+    double stage_ms[RF_STAGE_N] = {0};
+    uint32_t timed_frames = 0;
+};
+
+namespace {
+
+rf_status cuda_fail(rf_ctx *c, cudaError_t e, const char *what) {
+    if (c) snprintf(c->last_error, sizeof c->last_error, "%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? RF_ERR_OOM : RF_ERR_CUDA;
+}
+
+#define CK(call)                                                  \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+rf_status ensure(rf_ctx *ctx, DevBuf &b, size_t bytes) {
+    if (bytes <= b.cap && b.p) return RF_OK;
+    size_t cap = b.cap ? b.cap : 4096;
+    while (cap < bytes) cap *= 2;
+    if (b.p) {
+        CK(cudaStreamSynchronize(ctx->stream));  // the old buffer may still be in use
+        CK(cudaFree(b.p));
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    CK(cudaMalloc(&b.p, cap));
+    b.cap = cap;
+    return RF_OK;
+}
+
+template <class T>
+T *P(DevBuf &b) {
+    return reinterpret_cast<T *>(b.p);
+}
+
+bool is_pot(uint32_t x) { return x && !(x & (x - 1)); }
+
+uint32_t nattr_for(int32_t shader) {
+    switch (shader) {
+        case RF_SHADER_FLAT: return 0;
+        case RF_SHADER_TEXTURED: return 2;
+        case RF_SHADER_TEX_GOURAUD: return 5;
+        default: return 3;
+    }
+}
+
+uint32_t pack_px(uint32_t c, int32_t fmt) {
+    const uint32_t r = c & 0xFFu, g = (c >> 8) & 0xFFu, b = (c >> 16) & 0xFFu, a = c >> 24;
+    switch (fmt) {
+        case RF_ARGB8888: return (a << 24) | (r << 16) | (g << 8) | b;
+        case RF_XRGB8888: return (r << 16) | (g << 8) | b;
+        case RF_RGBA8888: return (r << 24) | (g << 16) | (b << 8) | a;
+        default: return (b << 24) | (g << 16) | (r << 8) | a;
+    }
+}
+
+void add_stats(rf_stats &a, const rf_stats &b) {
+    a.calls += b.calls; a.prims_i += b.prims_i; a.prims_o += b.prims_o;
+    a.verts_i += b.verts_i; a.verts_o += b.verts_o; a.frags_i += b.frags_i;
+    a.frags_o += b.frags_o; a.oob += b.oob;
+}
+
+// Device stats + overflow counters + host counts = the running total.
+rf_status read_totals(rf_ctx *ctx, rf_stats &tot) {
+    StatsDev sd{};
+    uint32_t cnt[RF_CNT_N] = {0};
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->stats.p) CK(cudaMemcpy(&sd, ctx->stats.p, sizeof sd, cudaMemcpyDeviceToHost));
+    if (ctx->counters.p) CK(cudaMemcpy(cnt, ctx->counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
+    tot = ctx->host_acc;
+    tot.prims_o += sd.prims_o;
+    tot.verts_o += sd.verts_o;
+    tot.frags_i += sd.frags_i;
+    tot.frags_o += sd.frags_o;
+    tot.oob += sd.oob + cnt[RF_CNT_POOLOVF] + cnt[RF_CNT_POLYOVF] + cnt[RF_CNT_BADIDX];
+    return RF_OK;
+}
+
+rf_status init_stats(rf_ctx *ctx) {
+    if (ctx->stats.p) return RF_OK;
+    rf_status s = ensure(ctx, ctx->stats, sizeof(StatsDev));
+    if (s) return s;
+    s = ensure(ctx, ctx->counters, RF_CNT_N * 4);
+    if (s) return s;
+    CK(cudaMemsetAsync(ctx->stats.p, 0, sizeof(StatsDev), ctx->stream));
+    CK(cudaMemsetAsync(ctx->counters.p, 0, RF_CNT_N * 4, ctx->stream));
+    return RF_OK;
+}
+
+// One frame: a single job (target) with ndraws draws, in order.
+rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const float vp[16],
+                  Target &tg, const rf_context_flags *fl) {
+    if (!vp || !fl) return RF_ERR_BAD_ARG;
+    rf_status st = init_stats(ctx);
+    if (st) return st;
+    auto &hd = ctx->hdraws;
+    hd.clear();
+    hd.reserve(ndraws);
+    uint64_t nv = 0, nt = 0;
+    for (uint32_t i = 0; i < ndraws; ++i) {
+        const rf_draw &dr = draws[i];
+        auto mit = ctx->meshes.find(dr.mesh);
+        if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+        const Mesh &m = mit->second;
+        if (dr.shader < RF_SHADER_FLAT || dr.shader > RF_SHADER_GOURAUD_SRGB) return RF_ERR_BAD_ARG;
+        if (m.nattr != nattr_for(dr.shader)) return RF_ERR_BAD_ARG;
+        DrawDev d{};
+        d.verts = m.verts;
+        d.idx = m.idx;
+        d.nverts = m.nverts;
+        d.ntri = m.ntri;
+        d.pos_dim = m.pos_dim;
+        d.nattr = m.nattr;
+        d.stride = m.pos_dim + m.nattr;
+        d.shader = dr.shader;
+        d.sampler = (int32_t)dr.uniforms.sampler;
+        d.flat_rgba = dr.uniforms.flat_rgba;
+        if (dr.shader == RF_SHADER_TEXTURED || dr.shader == RF_SHADER_TEX_GOURAUD) {
+            auto tit = ctx->textures.find(dr.uniforms.texture);
+            if (tit == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+            if (d.sampler < RF_SAMPLER_REPEAT_POT || d.sampler > RF_SAMPLER_ONCE) return RF_ERR_BAD_ARG;
+            if (d.sampler == RF_SAMPLER_REPEAT_POT && (!is_pot(tit->second.w) || !is_pot(tit->second.h)))
+                return RF_ERR_NON_POT_TEXTURE;
+            d.tex = tit->second.texels;
+            d.tw = tit->second.w;
+            d.th = tit->second.h;
+        }
+        d.vert_base = (uint32_t)nv;
+        d.tri_base = (uint32_t)nt;
+        d.job = 0;
+        memcpy(d.mvp, dr.uniforms.mvp, sizeof d.mvp);
+        nv += m.nverts;
+        nt += m.ntri;
+        hd.push_back(d);
+    }
+    if (nv > 0xFFFFFFF0ull || nt > 0x7FFFFFF0ull) return RF_ERR_BAD_ARG;
+    // Host-side counts (render.rs:152-155).
+    ctx->host_acc.calls += ndraws;
+    ctx->host_acc.prims_i += nt;
+    ctx->host_acc.verts_i += nv;
+
+    const uint32_t TW = ctx->tile_w;
+    JobDev J{};
+    J.color = tg.color;
+    J.depth = tg.depth;
+    J.w = tg.w;
+    J.h = tg.h;
+    J.pixfmt = tg.fmt;
+    J.depth_test = fl->depth_test;
+    J.color_write = fl->color_write;
+    J.depth_write = fl->depth_write;
+    J.face_cull = fl->face_cull;
+    J.tiles_x = (tg.w + TW - 1) / TW;
+    J.tiles_y = (tg.h + RF_TILE_H - 1) / RF_TILE_H;
+    J.tile_base = 0;
+    J.tri_base = 0;
+    J.ntri = (uint32_t)nt;
+    J.mask_words = (uint32_t)((nt + 31) / 32);
+    J.mask_base = 0;
+    J.clear_flags = tg.clear_flags;
+    J.clear_px = tg.clear_px;
+    J.clear_z = tg.clear_z;
+    memcpy(J.vp, vp, sizeof J.vp);
+    const uint32_t ntiles = J.tiles_x * J.tiles_y;
+    const size_t mask_words = (size_t)ntiles * J.mask_words;
+
+    if (nt == 0 || nv == 0) {
+        // Nothing to draw; a pending clear still lands on the next read.
+        return RF_OK;
+    }
+    if ((st = ensure(ctx, ctx->draws, hd.size() * sizeof(DrawDev)))) return st;
+    if ((st = ensure(ctx, ctx->jobs, sizeof(JobDev)))) return st;
+    if ((st = ensure(ctx, ctx->cpos, nv * sizeof(float4)))) return st;
+    if ((st = ensure(ctx, ctx->coc, nv))) return st;
+    if ((st = ensure(ctx, ctx->tcnt, nt * 4))) return st;
+    if ((st = ensure(ctx, ctx->toff, nt * 4))) return st;
+    if ((st = ensure(ctx, ctx->tpoly, nt * 4))) return st;
+    const uint32_t pool_cap = (uint32_t)nt;
+    if ((st = ensure(ctx, ctx->pool, (size_t)pool_cap * RF_POLY_STORE * sizeof(PolyVert)))) return st;
+    if ((st = ensure(ctx, ctx->prims, (size_t)nt * RF_MAX_FAN * sizeof(PrimRec)))) return st;
+    if ((st = ensure(ctx, ctx->mask, mask_words * 4))) return st;
+    if ((st = ensure(ctx, ctx->scan, rfk::scan_scratch_words((uint32_t)nt) * 4))) return st;
+
+    cudaStream_t s = ctx->stream;
+    std::vector<cudaEvent_t> ev;
+    if (ctx->timing) {
+        for (int i = 0; i <= RF_STAGE_N; ++i) {
+            cudaEvent_t e;
+            if (!ctx->ev_free.empty()) {
+                e = ctx->ev_free.back();
+                ctx->ev_free.pop_back();
+            } else {
+                CK(cudaEventCreate(&e));
+            }
+            ev.push_back(e);
+        }
+    }
+    auto mark = [&](int i) -> cudaError_t {
+        return ctx->timing ? cudaEventRecord(ev[i], s) : cudaSuccess;
+    };
+    CK(cudaMemcpyAsync(ctx->draws.p, hd.data(), hd.size() * sizeof(DrawDev), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->jobs.p, &J, sizeof J, cudaMemcpyHostToDevice, s));
+    uint32_t *counters = P<uint32_t>(ctx->counters);
+    CK(cudaMemsetAsync(counters + RF_CNT_POOL, 0, 4, s));
+    CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
+    CK(cudaMemsetAsync(ctx->mask.p, 0, mask_words * 4, s));
+    const DrawDev *dd = P<DrawDev>(ctx->draws);
+    const JobDev *jd = P<JobDev>(ctx->jobs);
+    CK(mark(RF_STAGE_VERTEX));
+    CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                          ctx->nsm, s));
+    CK(mark(RF_STAGE_CLIP));
+    CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                        P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
+                        pool_cap, counters, ctx->nsm, s));
+    CK(mark(RF_STAGE_SCAN));
+    CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
+                        P<uint32_t>(ctx->scan), counters + RF_CNT_PRIMS, s));
+    CK(mark(RF_STAGE_SETUP));
+    CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
+                         P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
+                         P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<uint32_t>(ctx->mask),
+                         P<StatsDev>(ctx->stats), ctx->nsm, s));
+    CK(mark(RF_STAGE_RASTER));
+    CK(rfk::launch_raster(TW, jd, 1, dd, P<PrimRec>(ctx->prims), P<uint32_t>(ctx->tcnt),
+                          P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles,
+                          counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->warps, ctx->nsm, s));
+    CK(mark(RF_STAGE_N));
+    if (ctx->timing) ctx->ev_pending.push_back(ev);
+    tg.clear_flags = 0;  // the raster pass wrote the pending clear
+    return RF_OK;
+}
+
+rf_status flush_clear(rf_ctx *ctx, Target &tg) {
+    if (!tg.clear_flags) return RF_OK;
+    CK(rfk::launch_fill(tg.color, tg.depth, (size_t)tg.w * tg.h, tg.clear_px, tg.clear_z,
+                        tg.clear_flags, ctx->nsm, ctx->stream));
+    tg.clear_flags = 0;
+    return RF_OK;
+}
+
+rf_status finish_call(rf_ctx *ctx, rf_stats *out) {
+    if (!out) return RF_OK;
+    rf_stats tot{};
+    rf_status st = read_totals(ctx, tot);
+    if (st) return st;
+    rf_stats d{};
+    d.calls = tot.calls - ctx->taken.calls;
+    d.prims_i = tot.prims_i - ctx->taken.prims_i;
+    d.prims_o = tot.prims_o - ctx->taken.prims_o;
+    d.verts_i = tot.verts_i - ctx->taken.verts_i;
+    d.verts_o = tot.verts_o - ctx->taken.verts_o;
+    d.frags_i = tot.frags_i - ctx->taken.frags_i;
+    d.frags_o = tot.frags_o - ctx->taken.frags_o;
+    d.oob = tot.oob - ctx->taken.oob;
+    ctx->taken = tot;
+    *out = d;
+    return RF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rf_status_str(rf_status s) {
+    switch (s) {
+        case RF_OK: return "ok";
+        case RF_ERR_BAD_HANDLE: return "bad handle";
+        case RF_ERR_BAD_ARG: return "bad argument";
+        case RF_ERR_NON_POT_TEXTURE: return "texture dimensions must be powers of two";
+        case RF_ERR_OOM: return "out of device memory";
+        case RF_ERR_OVER_BUDGET: return "over memory budget";
+        case RF_ERR_OVERFLOW: return "overflow";
+        case RF_ERR_TIMEOUT: return "timeout";
+        case RF_ERR_CUDA: return "cuda error";
+        case RF_ERR_NO_DEVICE: return "no cuda device";
+        default: return "unknown status";
+    }
+}
+
+rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out) {
+    if (!out) return RF_ERR_BAD_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return RF_ERR_NO_DEVICE;
+    }
+    rf_ctx *ctx = new (std::nothrow) rf_ctx();
+    if (!ctx) return RF_ERR_OOM;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cuda_stream) {
+        ctx->stream = (cudaStream_t)cuda_stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete ctx;
+            return RF_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    *out = ctx;
+    return RF_OK;
+}
+
+rf_status rf_ctx_destroy(rf_ctx *ctx) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); }
+    for (auto &kv : ctx->textures) cudaFree(kv.second.texels);
+    for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); }
+    DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
+                      &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
+                      &ctx->counters, &ctx->stats};
+    for (DevBuf *b : bufs) cudaFree(b->p);
+    for (auto &ev : ctx->ev_pending)
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RF_OK;
+}
+
+rf_status rf_ctx_sync(rf_ctx *ctx) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return RF_OK;
+}
+
+rf_status rf_ctx_take_stats(rf_ctx *ctx, rf_stats *out) {
+    if (!ctx || !out) return RF_ERR_BAD_ARG;
+    rf_stats d{};
+    rf_status st = finish_call(ctx, &d);
+    if (st) return st;
+    add_stats(*out, d);
+    return RF_OK;
+}
+
+rf_status rf_ctx_set_timing(rf_ctx *ctx, int32_t enable) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    ctx->timing = enable != 0;
+    return RF_OK;
+}
+
+rf_status rf_ctx_stage_ms(rf_ctx *ctx, double out[RF_STAGE_N], uint32_t *frames) {
+    if (!ctx || !out) return RF_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (auto &ev : ctx->ev_pending) {
+        for (int i = 0; i < RF_STAGE_N; ++i) {
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+            ctx->stage_ms[i] += ms;
+        }
+        for (cudaEvent_t e : ev) ctx->ev_free.push_back(e);
+        ctx->timed_frames += 1;
+    }
+    ctx->ev_pending.clear();
+    for (int i = 0; i < RF_STAGE_N; ++i) {
+        out[i] += ctx->stage_ms[i];
+        ctx->stage_ms[i] = 0.0;
+    }
+    if (frames) *frames = ctx->timed_frames;
+    ctx->timed_frames = 0;
+    return RF_OK;
+}
+
+rf_status rf_ctx_set_tiling(rf_ctx *ctx, uint32_t tile_w, uint32_t warps) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    if (tile_w && tile_w != 8 && tile_w != 16 && tile_w != 32 && tile_w != 64) return RF_ERR_BAD_ARG;
+    if (warps && (warps > RF_RASTER_MAX_THREADS / 32)) return RF_ERR_BAD_ARG;
+    if (tile_w) ctx->tile_w = tile_w;
+    if (warps) ctx->warps = warps;
+    return RF_OK;
+}
+
+rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
+                         uint32_t nattr, const uint32_t *idx, uint32_t ntri, rf_mesh *out) {
+    if (!ctx || !out || (pos_dim != 3 && pos_dim != 4) || nattr > RF_MAX_ATTR) return RF_ERR_BAD_ARG;
+    if ((nverts && !verts) || (ntri && !idx)) return RF_ERR_BAD_ARG;
+    for (uint64_t i = 0; i < 3ull * ntri; ++i)
+        if (idx[i] >= nverts) return RF_ERR_BAD_ARG;  // `vs[i]` would panic (prim.rs:17-19)
+    Mesh m;
+    m.nverts = nverts;
+    m.ntri = ntri;
+    m.pos_dim = pos_dim;
+    m.nattr = nattr;
+    const size_t vb = (size_t)nverts * (pos_dim + nattr) * 4, ib = (size_t)ntri * 12;
+    if (vb) CK(cudaMalloc(&m.verts, vb));
+    if (ib) CK(cudaMalloc(&m.idx, ib));
+    if (vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
+    if (ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const uint64_t h = ctx->next_handle++;
+    ctx->meshes[h] = m;
+    *out = h;
+    return RF_OK;
+}
+
+rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->meshes.find(mesh);
+    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    Mesh &m = it->second;
+    if (idx)
+        for (uint64_t i = 0; i < 3ull * m.ntri; ++i)
+            if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
+    const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * 12;
+    if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
+    if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return RF_OK;
+}
+
+rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->meshes.find(mesh);
+    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(it->second.verts);
+    cudaFree(it->second.idx);
+    ctx->meshes.erase(it);
+    return RF_OK;
+}
+
+rf_status rf_texture_upload(rf_ctx *ctx, const uint32_t *rgba, uint32_t w, uint32_t h,
+                            rf_texture *out) {
+    if (!ctx || !out || !rgba || !w || !h) return RF_ERR_BAD_ARG;
+    Texture t;
+    t.w = w;
+    t.h = h;
+    const size_t b = (size_t)w * h * 4;
+    CK(cudaMalloc(&t.texels, b));
+    CK(cudaMemcpyAsync(t.texels, rgba, b, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const uint64_t hd = ctx->next_handle++;
+    ctx->textures[hd] = t;
+    *out = hd;
+    return RF_OK;
+}
+
+rf_status rf_texture_destroy(rf_ctx *ctx, rf_texture tex) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->textures.find(tex);
+    if (it == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(it->second.texels);
+    ctx->textures.erase(it);
+    return RF_OK;
+}
+
+rf_status rf_target_create(rf_ctx *ctx, uint32_t w, uint32_t h, int32_t pixfmt, int32_t has_depth,
+                           rf_target *out) {
+    if (!ctx || !out || !w || !h || w > 65536 || h > 65536) return RF_ERR_BAD_ARG;
+    if (pixfmt < RF_ARGB8888 || pixfmt > RF_BGRA8888) return RF_ERR_BAD_ARG;
+    Target t;
+    t.w = w;
+    t.h = h;
+    t.fmt = pixfmt;
+    const size_t n = (size_t)w * h;
+    CK(cudaMalloc(&t.color, n * 4));
+    CK(cudaMemsetAsync(t.color, 0, n * 4, ctx->stream));
+    if (has_depth) {
+        CK(cudaMalloc(&t.depth, n * 4));
+        CK(cudaMemsetAsync(t.depth, 0, n * 4, ctx->stream));
+    }
+    const uint64_t hd = ctx->next_handle++;
+    ctx->targets[hd] = t;
+    *out = hd;
+    return RF_OK;
+}
+
+rf_status rf_target_destroy(rf_ctx *ctx, rf_target t) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->targets.find(t);
+    if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(it->second.color);
+    cudaFree(it->second.depth);
+    ctx->targets.erase(it);
+    return RF_OK;
+}
+
+rf_status rf_target_clear(rf_ctx *ctx, rf_target t, const uint32_t *clear_rgba,
+                          const float *depth_clear) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->targets.find(t);
+    if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    Target &tg = it->second;
+    if (clear_rgba) {
+        tg.clear_flags |= 1u;
+        tg.clear_px = pack_px(*clear_rgba, tg.fmt);
+    }
+    if (depth_clear && tg.depth) {
+        tg.clear_flags |= 2u;
+        volatile float one = 1.0f;
+        tg.clear_z = one / *depth_clear;  // f32::recip
+    }
+    return RF_OK;
+}
+
+rf_status rf_target_write(rf_ctx *ctx, rf_target t, const uint32_t *color, const float *depth) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->targets.find(t);
+    if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    Target &tg = it->second;
+    rf_status st = flush_clear(ctx, tg);
+    if (st) return st;
+    const size_t n = (size_t)tg.w * tg.h * 4;
+    if (color) CK(cudaMemcpyAsync(tg.color, color, n, cudaMemcpyHostToDevice, ctx->stream));
+    if (depth && tg.depth) CK(cudaMemcpyAsync(tg.depth, depth, n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return RF_OK;
+}
+
+rf_status rf_target_read(rf_ctx *ctx, rf_target t, uint32_t *color, float *depth) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->targets.find(t);
+    if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    Target &tg = it->second;
+    rf_status st = flush_clear(ctx, tg);
+    if (st) return st;
+    const size_t n = (size_t)tg.w * tg.h * 4;
+    if (color) CK(cudaMemcpyAsync(color, tg.color, n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (depth && tg.depth) CK(cudaMemcpyAsync(depth, tg.depth, n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return RF_OK;
+}
+
+rf_status rf_render(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_uniforms *uniforms,
+                    const float viewport[16], rf_target target, const rf_context_flags *flags,
+                    rf_stats *stats) {
+    if (!ctx || !uniforms) return RF_ERR_BAD_ARG;
+    rf_draw d;
+    memset(&d, 0, sizeof d);
+    d.mesh = mesh;
+    d.shader = shader;
+    d.uniforms = *uniforms;
+    return rf_render_draws(ctx, &d, 1, viewport, target, flags, stats);
+}
+
+rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
+                          const float viewport[16], rf_target target,
+                          const rf_context_flags *flags, rf_stats *stats) {
+    if (!ctx || (ndraws && !draws)) return RF_ERR_BAD_ARG;
+    auto it = ctx->targets.find(target);
+    if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    if (flags && (flags->depth_test < RF_DEPTH_NONE || flags->depth_test > RF_DEPTH_GREATER ||
+                  flags->face_cull < RF_CULL_NONE || flags->face_cull > RF_CULL_FRONT))
+        return RF_ERR_BAD_ARG;
+    rf_status st = run_job(ctx, draws, ndraws, viewport, it->second, flags);
+    if (st) return st;
+    return finish_call(ctx, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// rf_kernels.cuh — constants and launch helpers shared by rf_kernels.cu and
+// the C-ABI driver rf_api.cu.
+#ifndef RF_KERNELS_CUH
+#define RF_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rf_internal.cuh"
+
+// Mirrors of the public enums in include/rfgpu.h.
+#define RF_K_FLAT 0
+#define RF_K_GOURAUD 1
+#define RF_K_TEXTURED 2
+#define RF_K_TEX_GOURAUD 3
+#define RF_K_GOURAUD_SRGB 4
+#define RF_K_REPEAT_POT 0
+#define RF_K_CLAMP 1
+#define RF_K_ONCE 2
+#define RF_K_ARGB8888 0
+#define RF_K_XRGB8888 1
+#define RF_K_RGBA8888 2
+#define RF_K_BGRA8888 3
+#define RF_K_DEPTH_NONE 0
+#define RF_K_DEPTH_LESS 1
+#define RF_K_DEPTH_EQUAL 2
+#define RF_K_DEPTH_GREATER 3
+#define RF_K_CULL_NONE 0
+#define RF_K_CULL_BACK 1
+#define RF_K_CULL_FRONT 2
+
+#define RF_NO_POLY 0xFFFFFFFFu
+// Scanline y origins beyond +-2^22 px are outside the supported domain: the
+// row arithmetic y0r + j must stay exact in f32.  Such halves count in oob.
+#define RF_MAX_COORD 4194304.0f
+#define RF_RASTER_MAX_THREADS 256
+
+// counters[] slots
+#define RF_CNT_POOL 0     // pool slots used
+#define RF_CNT_POOLOVF 1  // polygons dropped for lack of pool slots
+#define RF_CNT_POLYOVF 2  // polygons that exceeded RF_POLY_CAP vertices
+#define RF_CNT_BADIDX 3   // triangles with an out-of-range vertex index
+#define RF_CNT_PRIMS 4    // total output prims (scan total)
+#define RF_CNT_QUEUE 5    // tile queue head
+#define RF_CNT_N 8
+
+namespace rfk {
+cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
+                          uint8_t *coc, int nsm, cudaStream_t s);
+cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
+                        const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, PolyVert *pool,
+                        uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s);
+size_t scan_scratch_words(uint32_t n);
+cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch,
+                        uint32_t *total, cudaStream_t s);
+cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
+                         uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
+                         const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
+                         PrimRec *prims, uint32_t *mask, StatsDev *stats, int nsm, cudaStream_t s);
+cudaError_t launch_raster(uint32_t tile_w, const JobDev *jobs, uint32_t nj, const DrawDev *draws,
+                          const PrimRec *prims, const uint32_t *tcnt, const uint32_t *toff,
+                          const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
+                          StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s);
+cudaError_t launch_fill(uint32_t *color, float *depth, size_t n, uint32_t px, float z,
+                        uint32_t flags, int nsm, cudaStream_t s);
+}  // namespace rfk
+
+#endif

@@ -21,10 +21,16 @@ def _dot(a, b):
 
 
 def compose(m, n):
-    """m.compose(n): apply n first, then m (mat.rs:268-283)."""
+    """m.compose(n): apply n first, then m (mat.rs:268-283).
+
+    Element (j, i) is dot(m[j], column i of n) folded from 0.0 in k order;
+    works on stacks of matrices (..., 4, 4)."""
     m = np.asarray(m, f32)
-    nt = np.asarray(n, f32).T
-    return np.array([[_dot(m[j], nt[i]) for i in range(4)] for j in range(4)], f32)
+    n = np.asarray(n, f32)
+    acc = np.zeros(np.broadcast_shapes(m.shape, n.shape), f32)
+    for k in range(4):
+        acc = (acc + m[..., :, k, None] * n[..., None, k, :]).astype(f32)
+    return acc
 
 
 def then(m, n):
