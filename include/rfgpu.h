@@ -173,6 +173,39 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
                           const float viewport[16], rf_target target,
                           const rf_context_flags *flags, rf_stats *stats);
 
+/* ---- rendering without device allocation ------------------------------
+ * No counterpart in the reference: retrofire allocates freely on the CPU.
+ * For callers that must not call cudaMalloc while rendering — a frame loop
+ * held to a fixed, pre-reserved device-memory budget, a plugin inside a host
+ * application that owns all allocations, code recording into a CUDA graph.
+ * One render() call like rf_render, but every buffer is the caller's device
+ * memory (verts, idx, texture, colour, optional depth) and the temporaries
+ * live in a fixed scratch area of RF_NOALLOC_SCRATCH_BYTES compiled into the
+ * library, which every GPU that loads the library keeps until exit.  The
+ * call allocates nothing.  Limits: ntri <= RF_NOALLOC_MAX_TRIS, nverts <=
+ * RF_NOALLOC_MAX_VERTS, w <= RF_NOALLOC_MAX_W, h <= RF_NOALLOC_MAX_H;
+ * larger inputs return RF_ERR_OVER_BUDGET.
+ * The first call on a device looks up the scratch area's device address
+ * (once per device, with that device current), so make that first call
+ * before any stream capture.  All calls share the one area: calls whose GPU
+ * work overlaps race and give wrong results — order them on one stream.
+ * clear_rgba / depth_clear (nullable) apply Frame::clear first.  stats,
+ * when non-NULL, waits for the stream and receives this call's stats.
+ * cuda_stream may be NULL (the legacy default stream). */
+#define RF_NOALLOC_MAX_TRIS 1024u
+#define RF_NOALLOC_MAX_VERTS 4096u
+#define RF_NOALLOC_MAX_W 1024u
+#define RF_NOALLOC_MAX_H 1024u
+#define RF_NOALLOC_SCRATCH_BYTES (2u << 20)
+rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint32_t pos_dim, uint32_t nattr,
+                            const uint32_t *idx, uint32_t ntri, int32_t shader,
+                            const float mvp[16], uint32_t flat_rgba, const uint32_t *tex,
+                            uint32_t tw, uint32_t th, uint32_t sampler, const float viewport[16],
+                            uint32_t *color, float *depth, uint32_t w, uint32_t h,
+                            int32_t pixfmt, const rf_context_flags *flags,
+                            const uint32_t *clear_rgba, const float *depth_clear,
+                            void *cuda_stream, rf_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

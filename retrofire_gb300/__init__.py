@@ -95,6 +95,12 @@ _SIGS = {
                   C.c_uint64, C.POINTER(Flags), C.POINTER(CStats)],
     "rf_render_draws": [_P, C.POINTER(Draw), C.c_uint32, C.POINTER(C.c_float), C.c_uint64,
                         C.POINTER(Flags), C.POINTER(CStats)],
+    # device pointers throughout; see include/rfgpu.h
+    "rf_render_noalloc": [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.c_uint32, C.c_int32,
+                          C.POINTER(C.c_float), C.c_uint32, _P, C.c_uint32, C.c_uint32,
+                          C.c_uint32, C.POINTER(C.c_float), _P, _P, C.c_uint32, C.c_uint32,
+                          C.c_int32, C.POINTER(Flags), C.POINTER(C.c_uint32),
+                          C.POINTER(C.c_float), _P, C.POINTER(CStats)],
 }
 
 _lib = None

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "librfgpu.so")
-SRCS = ["rf_kernels.cu", "rf_api.cu"]
+SRCS = ["rf_kernels.cu", "rf_api.cu", "rf_noalloc.cu"]
 HDRS = ["rf_exact.cuh", "rf_internal.cuh", "rf_kernels.cuh"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
