@@ -196,7 +196,7 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
 #define RF_NOALLOC_MAX_VERTS 4096u
 #define RF_NOALLOC_MAX_W 1024u
 #define RF_NOALLOC_MAX_H 1024u
-#define RF_NOALLOC_SCRATCH_BYTES (2u << 20)
+#define RF_NOALLOC_SCRATCH_BYTES (8u << 20)
 rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint32_t pos_dim, uint32_t nattr,
                             const uint32_t *idx, uint32_t ntri, int32_t shader,
                             const float mvp[16], uint32_t flat_rgba, const uint32_t *tex,

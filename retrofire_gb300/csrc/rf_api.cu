@@ -291,10 +291,14 @@ rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const floa
     CK(mark(RF_STAGE_SETUP));
     CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
                          P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
-                         P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<uint32_t>(ctx->mask),
+                         P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), counters + RF_CNT_PRIMS, P<uint32_t>(ctx->mask),
                          P<StatsDev>(ctx->stats), ctx->nsm, s));
     CK(mark(RF_STAGE_RASTER));
-    CK(rfk::launch_raster(TW, jd, 1, dd, P<PrimRec>(ctx->prims), P<uint32_t>(ctx->tcnt),
+    int kind = hd[0].shader;
+    for (const DrawDev &d : hd)
+        if (d.shader != kind) kind = RF_K_ANY;
+    const bool fast = tg.depth && fl->depth_test == RF_DEPTH_LESS && fl->color_write && fl->depth_write;
+    CK(rfk::launch_raster(TW, kind, fast, jd, 1, dd, P<PrimRec>(ctx->prims), P<uint32_t>(ctx->tcnt),
                           P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles,
                           counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->warps, ctx->nsm, s));
     CK(mark(RF_STAGE_N));

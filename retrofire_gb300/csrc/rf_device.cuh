@@ -1,0 +1,50 @@
+// rf_device.cuh — device helpers shared by the kernel translation units.
+#ifndef RF_DEVICE_CUH
+#define RF_DEVICE_CUH
+
+#include <cuda_runtime.h>
+
+#include "rf_exact.cuh"
+#include "rf_internal.cuh"
+#include "rf_kernels.cuh"
+
+namespace rfd {
+using namespace rfx;
+
+// Largest i with key(i) <= x over a sorted array of n records.
+template <class F>
+__device__ __forceinline__ uint32_t upper_index(uint32_t n, uint32_t x, F key) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (key(mid) <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Warp-aggregated 64-bit counter add (all 32 lanes must call).
+__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned long long v,
+                                             bool same_dst) {
+    if (same_dst) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+    } else if (v) {
+        atomicAdd(dst, v);
+    }
+}
+
+// Row quantity r of half H after j scanlines (see HalfRec): one of the two
+// precomputed single-binade runs, else the general loop from the second.
+__device__ __forceinline__ float row_value(const HalfRec *__restrict__ H, int r, uint32_t j) {
+    const uint32_t e0 = H->e0[r];
+    if (j <= e0) return u2f(H->b0[r] + j * (uint32_t)H->i0[r]);
+    const uint32_t j1 = j - e0 - 1u;
+    if (j <= H->e1[r]) return u2f(H->b1[r] + j1 * (uint32_t)H->i1[r]);
+    return seq_add_n(u2f(H->b1[r]), H->d[r], j1);
+}
+
+}  // namespace rfd
+
+#endif

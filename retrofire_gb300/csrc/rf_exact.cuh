@@ -22,8 +22,10 @@
 
 #if defined(__CUDACC__)
 #define RF_HD __host__ __device__ __forceinline__
+#define RF_HD_COLD static __host__ __device__ __noinline__
 #else
 #define RF_HD inline
+#define RF_HD_COLD static inline
 #endif
 
 namespace rfx {
@@ -127,6 +129,20 @@ RF_HD float dot4(const float *a, const float *b) {
 // Lerp (math.rs:196-198): a + (b - a) * t.
 RF_HD float lerp(float a, float b, float t) { return fadd(a, fmul(fsub(b, a), t)); }
 
+// floor(a / b) for 0 <= a < 2^24, 1 <= b < 2^24, without an integer divide on
+// the device: the float quotient is within a few units (relative error of
+// the reciprocal and the product), then corrected exactly.
+RF_HD uint32_t udiv24(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    uint32_t q = (uint32_t)__fmul_rz((float)a, __frcp_rn((float)b));
+    while ((uint64_t)q * b > a) --q;
+    while ((uint64_t)(q + 1) * b <= a) ++q;
+    return q;
+#else
+    return a / b;
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // rf_seq_add_n: k sequential additions s += d, exactly.
 //
@@ -142,7 +158,7 @@ RF_HD float lerp(float a, float b, float t) { return fadd(a, fmul(fsub(b, a), t)
 // the hardware adder, so every boundary rounding is the IEEE one by
 // construction.  A step that leaves s unchanged is a fixed point.
 // ---------------------------------------------------------------------------
-RF_HD float seq_add_n(float s, float d, uint32_t k) {
+RF_HD_COLD float seq_add_n(float s, float d, uint32_t k) {
     while (k != 0) {
         const uint32_t sb = f2u(s), db = f2u(d);
         const uint32_t se = (sb >> 23) & 0xFFu, de = (db >> 23) & 0xFFu;
@@ -203,13 +219,13 @@ RF_HD float seq_add_n(float s, float d, uint32_t k) {
                     const uint32_t mag = ((ee - 1u) << 23) + m + (uint32_t)total;
                     return u2f((sb & 0x80000000u) | mag);
                 }
-                n = (hi - m) / inc;
+                n = udiv24(hi - m, inc);
             } else {
                 if ((uint64_t)m >= total + lo) {
                     const uint32_t mag = ((ee - 1u) << 23) + m - (uint32_t)total;
                     return u2f((sb & 0x80000000u) | mag);
                 }
-                n = m >= lo ? (m - lo) / inc : 0u;
+                n = m >= lo ? udiv24(m - lo, inc) : 0u;
             }
             if (n != 0u) {  // n < k: advance to the edge of the binade
                 const uint32_t mm = grow ? m + n * inc : m - n * inc;
@@ -224,6 +240,95 @@ RF_HD float seq_add_n(float s, float d, uint32_t k) {
         s = t;
     }
     return s;
+}
+
+// ---------------------------------------------------------------------------
+// The single-binade run, precomputed.  fast_params(s, d) returns dinc and
+// kmax such that for every k <= kmax the k-step sum is the bit pattern of s
+// plus k * dinc (two's complement on the whole pattern: the sign never
+// changes inside a run).  kmax = 0 when no run applies (then only k = 0 is
+// covered).  Used for per-row steps, whose start and step are fixed per
+// half-triangle: a row anywhere in the triangle costs one multiply-add.
+// ---------------------------------------------------------------------------
+RF_HD void fast_params(float s, float d, int32_t &dinc, uint32_t &kmax) {
+    dinc = 0;
+    kmax = 0;
+    const uint32_t sb = f2u(s), db = f2u(d);
+    const uint32_t se = (sb >> 23) & 0xFFu, de = (db >> 23) & 0xFFu;
+    if (se == 0xFFu || de == 0xFFu || (db & 0x7FFFFFFFu) == 0u || (sb & 0x7FFFFFFFu) == 0u) return;
+    const uint32_t ee = se > 1u ? se : 1u;
+    const uint32_t m = (sb & 0x7FFFFFu) | (se ? 0x800000u : 0u);
+    const uint32_t md = (db & 0x7FFFFFu) | (de ? 0x800000u : 0u);
+    const int32_t ed = de > 1u ? (int32_t)de : 1;
+    const int32_t sh = (int32_t)ee - ed;
+    uint32_t q = 0, rem_up = 0, tie = 0;
+    if (sh <= 0) {
+        if (sh < -7) return;
+        q = md << (uint32_t)(-sh);
+    } else if (sh < 25) {
+        q = md >> (uint32_t)sh;
+        const uint32_t rem = md & ((1u << (uint32_t)sh) - 1u);
+        const uint32_t half = 1u << (uint32_t)(sh - 1);
+        rem_up = rem > half;
+        tie = rem == half;
+    }
+    const bool grow = ((sb ^ db) >> 31) == 0u;
+    const uint32_t lo = se > 1u ? 0x800001u : 1u;
+    const uint32_t hi = 0xFFFFFFu;
+    uint32_t inc;
+    if (tie) {
+        if (m & 1u) return;
+        inc = q + (q & 1u);
+    } else {
+        inc = q + rem_up;
+    }
+    if (inc == 0u) {
+        if (grow || m >= lo) kmax = 0xFFFFFFFFu;  // fixed point
+        return;
+    }
+    if (inc > hi) return;
+    if (grow) {
+        kmax = udiv24(hi - m, inc);
+        dinc = (int32_t)inc;
+    } else {
+        kmax = m >= lo ? udiv24(m - lo, inc) : 0u;
+        dinc = -(int32_t)inc;
+    }
+}
+
+// k sequential additions with the single-binade run tried inline first and
+// the general loop out of line (it is rarely needed).
+RF_HD float jump(float s, float d, uint32_t k) {
+    if (k == 0u) return s;
+    const uint32_t sb = f2u(s), db = f2u(d);
+    const uint32_t se = (sb >> 23) & 0xFFu, de = (db >> 23) & 0xFFu;
+    if (se - 2u < 253u && de - 1u < 254u) {  // s normal above the first binade, d normal
+        const uint32_t m = (sb & 0x7FFFFFu) | 0x800000u;
+        const uint32_t md = (db & 0x7FFFFFu) | 0x800000u;
+        const int32_t sh = (int32_t)se - (int32_t)de;
+        if (sh >= -7) {
+            uint32_t inc = 0;
+            bool ok = true;
+            if (sh <= 0) {
+                inc = md << (uint32_t)(-sh);
+            } else if (sh < 25) {
+                const uint32_t q = md >> (uint32_t)sh;
+                const uint32_t rem = md & ((1u << (uint32_t)sh) - 1u);
+                const uint32_t half = 1u << (uint32_t)(sh - 1);
+                ok = rem != half;  // ties take the general path
+                inc = q + (rem > half ? 1u : 0u);
+            }
+            if (ok) {
+                const uint64_t total = (uint64_t)inc * (uint64_t)k;
+                if (((sb ^ db) >> 31) == 0u) {
+                    if ((uint64_t)m + total <= 0xFFFFFFull) return u2f(sb + (uint32_t)total);
+                } else if ((uint64_t)m >= total + 0x800001ull) {
+                    return u2f(sb - (uint32_t)total);
+                }
+            }
+        }
+    }
+    return seq_add_n(s, d, k);
 }
 
 }  // namespace rfx

@@ -62,23 +62,36 @@ struct PolyVert {
     float a[RF_MAX_ATTR];
 };
 
-// One ScanlineIter after scan() (raster.rs:45-51, 248-302): rows
-// y0r, y0r+1, ... (n of them); left edge x and interpolated components
-// c[0] = screen z, c[1..] = attributes, stepped by dl per row; right edge x
-// stepped by drx; dvdx = per-pixel step.
+// One ScanlineIter after scan() (raster.rs:45-51, 248-302): rows y0r,
+// y0r+1, ... (n of them).  Row quantity r (RF_R_LX left edge x, RF_R_RX right
+// edge x, RF_R_C + c interpolated component c: c = 0 screen z, c >= 1 the
+// attributes) is the running sum start + j * d over rows.  Its exact value
+// is kept as two single-binade runs (rfx::fast_params): rows 0..e0[r] have
+// bits b0[r] + j * i0[r]; one explicit addition later, rows e0[r]+1..e1[r]
+// have bits b1[r] + (j - e0[r] - 1) * i1[r]; rows past e1[r] continue from
+// the second run with the general loop.  dvdx = per-pixel step.
+#define RF_R_LX 0
+#define RF_R_RX 1
+#define RF_R_C 2
+#define RF_NR (RF_R_C + RF_NC)
 struct HalfRec {
     float y0r;
     uint32_t n;
-    float lx, dlx, rx, drx;
-    float c[RF_NC];
-    float dc[RF_NC];
+    uint32_t b0[RF_NR];
+    int32_t i0[RF_NR];
+    uint32_t e0[RF_NR];
+    uint32_t b1[RF_NR];
+    int32_t i1[RF_NR];
+    uint32_t e1[RF_NR];
+    float d[RF_NR];
     float dvdx[RF_NC];
 };
 
 struct PrimRec {
     uint32_t draw;
     uint32_t live;  // 0: culled by the face-cull test
-    uint32_t pad_[2];
+    uint32_t tri;   // global input triangle it was clipped from
+    int32_t kind;   // shader kind of its draw
     HalfRec half[2];
 };
 

@@ -5,7 +5,9 @@
 //   k_clip     status + Sutherland-Hodgman count      clip.rs:245-301,350-400
 //   k_scan_*   order-preserving compaction offsets    (submission order)
 //   k_setup    to_screen, face cull, tri_fill/scan    prim.rs:62-88, raster.rs:185-302
-//              setup, row walk (stats), tile binning
+//              setup
+//   k_bin      scanline stats (frags.i, oob) and      raster.rs:80-114, target.rs:259-264
+//              tile binning, one warp per triangle
 //   k_raster   per-tile scan conversion, depth test,  raster.rs:80-114, target.rs:163-198
 //              fragment shading, pixel packing
 //   k_fill     Frame::clear without a later render    front/src/lib.rs:103-120
@@ -14,8 +16,10 @@
 #include "rf_exact.cuh"
 #include "rf_internal.cuh"
 #include "rf_kernels.cuh"
+#include "rf_device.cuh"
 
 using namespace rfx;
+using namespace rfd;
 
 namespace {
 
@@ -35,18 +39,6 @@ __device__ __forceinline__ uint32_t outcode(const float *p) {
     return oc;
 }
 
-// Largest i with key(i) <= x over a sorted array of n records.
-template <class F>
-__device__ __forceinline__ uint32_t upper_index(uint32_t n, uint32_t x, F key) {
-    uint32_t lo = 0, hi = n;
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (key(mid) <= x) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 __device__ __forceinline__ uint32_t nattr_of(int32_t shader) {
     switch (shader) {
         case RF_K_FLAT: return 0;
@@ -59,18 +51,6 @@ __device__ __forceinline__ uint32_t nattr_of(int32_t shader) {
 // (color.rs:628).
 __device__ __forceinline__ uint32_t zdiv_mask_of(int32_t shader) {
     return shader == RF_K_TEXTURED ? 0x3u : (shader == RF_K_TEX_GOURAUD ? 0x18u : 0u);
-}
-
-// Warp-aggregated 64-bit counter add (all 32 lanes must call).
-__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned long long v,
-                                             bool same_dst) {
-    if (same_dst) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-        if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
-    } else if (v) {
-        atomicAdd(dst, v);
-    }
 }
 
 }  // namespace
@@ -332,100 +312,60 @@ __device__ void scan_setup(float y0, float y1, const SV &l0, const SV &l1, const
     const float yt = fsub(y0r, y0);
     h.y0r = y0r;
     h.n = as_u32(fsub(y1r, y0r));
-    h.dlx = dlx;
-    h.drx = drx;
-    h.lx = fadd(l0.x, fmul(fsub(fadd(l0.x, dlx), l0.x), yt));
-    h.rx = fadd(r0.x, fmul(drx, yt));
+    float st[RF_NR];
+    h.d[RF_R_LX] = dlx;
+    h.d[RF_R_RX] = drx;
+    st[RF_R_LX] = fadd(l0.x, fmul(fsub(fadd(l0.x, dlx), l0.x), yt));
+    st[RF_R_RX] = fadd(r0.x, fmul(drx, yt));
     for (uint32_t c = 0; c < RF_NC; ++c) {
         if (c < nc) {
             const float dl = fmul(fsub(l1.c[c], l0.c[c]), recip_dy);
             const float dr = fmul(fsub(r1.c[c], r0.c[c]), recip_dy);
             const float l0s = fadd(l0.c[c], dl), r0s = fadd(r0.c[c], dr);
-            h.dc[c] = dl;
+            h.d[RF_R_C + c] = dl;
             h.dvdx[c] = fmul(fsub(r0s, l0s), rdx);
-            h.c[c] = fadd(l0.c[c], fmul(fsub(fadd(l0.c[c], dl), l0.c[c]), yt));
+            st[RF_R_C + c] = fadd(l0.c[c], fmul(fsub(fadd(l0.c[c], dl), l0.c[c]), yt));
         } else {
-            h.dc[c] = 0.0f;
+            h.d[RF_R_C + c] = 0.0f;
             h.dvdx[c] = 0.0f;
-            h.c[c] = 0.0f;
+            st[RF_R_C + c] = 0.0f;
         }
+    }
+    for (uint32_t r = 0; r < RF_NR; ++r) {
+        // Run 0 from the first row; run 1 after one explicit addition.
+        uint32_t k0, k1;
+        fast_params(st[r], h.d[r], h.i0[r], k0);
+        h.b0[r] = f2u(st[r]);
+        h.e0[r] = k0;
+        if (k0 == 0xFFFFFFFFu) {  // fixed point: run 0 covers every row
+            h.b1[r] = h.b0[r];
+            h.i1[r] = 0;
+            h.e1[r] = k0;
+            continue;
+        }
+        const float v1 = fadd(u2f(h.b0[r] + k0 * (uint32_t)h.i0[r]), h.d[r]);
+        fast_params(v1, h.d[r], h.i1[r], k1);
+        h.b1[r] = f2u(v1);
+        const uint64_t e1 = (uint64_t)k0 + 1u + k1;
+        h.e1[r] = e1 > 0xFFFFFFFEull ? 0xFFFFFFFEu : (uint32_t)e1;
     }
 }
 
-struct WalkAcc {
-    unsigned long long frags_i, oob;
-};
-
-// Walks the scanlines of one half exactly like ScanlineIter::next
-// (raster.rs:80-114) for the frags.i / oob counters of rasterize_fb
-// (target.rs:259-264), and marks the tiles its pixels touch.
-__device__ void walk_half(const HalfRec &h, const JobDev &J, uint32_t tw, uint32_t tl,
-                          uint32_t *__restrict__ mask, WalkAcc &acc) {
-    if (h.n == 0) return;
-    if (!(fabsf(h.y0r) < RF_MAX_COORD)) {  // outside the supported coordinate range
-        acc.oob += 1;
-        return;
-    }
-    float lx = h.lx, rx = h.rx, yf = h.y0r;
-    uint32_t band = 0xFFFFFFFFu, bx0 = 0, bx1 = 0;
-    const uint32_t word = tl >> 5, bit = 1u << (tl & 31);
-    auto flush = [&]() {
-        if (band != 0xFFFFFFFFu && bx1 > bx0) {
-            const uint32_t t0 = bx0 / tw, t1 = (bx1 - 1) / tw;
-            uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
-            for (uint32_t t = t0; t <= t1; ++t) atomicOr(row + (size_t)t * J.mask_words, bit);
-        }
-    };
-    for (uint32_t j = 0; j < h.n; ++j) {
-        const uint64_t y = as_usize(yf);
-        if (y >= J.h) {  // every later row is at least as low: all out of bounds
-            acc.oob += h.n - j;
-            break;
-        }
-        const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-        const uint64_t xs = as_usize(x0r);
-        uint64_t xe = as_usize(x1r);
-        if (xe < xs) xe = xs;
-        acc.frags_i += xe - xs;
-        if (xe > J.w) acc.oob += 1;
-        uint64_t nfr = xe - xs;
-        const uint32_t cnt = as_u32(fsub(x1r, x0r));
-        if (cnt < nfr) nfr = cnt;
-        if (nfr && xs < J.w) {
-            const uint32_t px0 = (uint32_t)xs;
-            const uint32_t px1 = (uint32_t)(xs + nfr < J.w ? xs + nfr : J.w);
-            const uint32_t b = (uint32_t)y / RF_TILE_H;
-            if (b != band) {
-                flush();
-                band = b;
-                bx0 = px0;
-                bx1 = px1;
-            } else {
-                bx0 = min(bx0, px0);
-                bx1 = max(bx1, px1);
-            }
-        }
-        lx = fadd(lx, h.dlx);
-        rx = fadd(rx, h.drx);
-        yf = fadd(yf, 1.0f);
-    }
-    flush();
-}
 }  // namespace
 
 __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
-                        const JobDev *__restrict__ jobs, uint32_t nt_total, uint32_t tile_w,
+                        const JobDev *__restrict__ jobs, uint32_t nt_total,
                         const float4 *__restrict__ cpos, const uint32_t *__restrict__ tcnt,
                         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ tpoly,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
-                        uint32_t *__restrict__ mask, StatsDev *__restrict__ stats) {
+                        StatsDev *__restrict__ stats) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < nt_total; base += stride) {
         const uint32_t gt = base + threadIdx.x;
         const bool active = gt < nt_total;
         const uint32_t cnt = active ? tcnt[gt] : 0u;
         uint32_t job = 0xFFFFFFFFu;
-        unsigned long long prims_o = 0, frags_i = 0, oob = 0;
+        unsigned long long prims_o = 0;
         if (cnt) {
             const uint32_t di = upper_index(nd, gt, [&](uint32_t i) { return draws[i].tri_base; });
             const DrawDev &d = draws[di];
@@ -437,7 +377,6 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
             const uint32_t zm = zdiv_mask_of(d.shader);
             const uint32_t slot = tpoly[gt];
             const uint32_t p0 = toff[gt];
-            WalkAcc acc{0, 0};
             for (uint32_t c = 0; c < cnt; ++c) {
                 // Gather the three clip-space vertices of this (fan) triangle.
                 float pos[3][4], at[3][RF_MAX_ATTR];
@@ -476,6 +415,8 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 PrimRec &P = prims[p0 + c];
                 P.draw = di;
                 P.live = culled ? 0u : 1u;
+                P.tri = gt;
+                P.kind = d.shader;
                 if (culled) continue;
                 prims_o += 1;
                 // raster.rs:185-224 tri_fill: stable sort by y (total_cmp).
@@ -496,12 +437,7 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 scan_setup(v1.y, v2.y, left, v2, right, v2, nc, h1);
                 P.half[0] = h0;
                 P.half[1] = h1;
-                const uint32_t tl = gt - J.tri_base;
-                walk_half(h0, J, tile_w, tl, mask, acc);
-                walk_half(h1, J, tile_w, tl, mask, acc);
             }
-            frags_i = acc.frags_i;
-            oob = acc.oob;
         }
         // Stats, aggregated per warp when all lanes share one job.
         const uint32_t hasjob = __ballot_sync(0xFFFFFFFFu, job != 0xFFFFFFFFu);
@@ -512,281 +448,142 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 StatsDev *S = stats + (same ? j0 : job);
                 warp_add_u64(&S->prims_o, prims_o, same);
                 warp_add_u64(&S->verts_o, 3ull * prims_o, same);
-                warp_add_u64(&S->frags_i, frags_i, same);
-                warp_add_u64(&S->oob, oob, same);
             }
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// K4: tile rasteriser.
-// A warp owns one tile of RF_TILE_H rows x TW columns at a time; lane r owns
-// row r of the tile for the whole tile, so per-pixel submission order is the
-// order in which the lane walks the triangle list — no atomics, no sorting.
-// Colour and depth sit in shared memory column-major (word x*32 + r): the
-// bank of every access is the lane id, whatever x each lane is at.
-// Each lane enters its row with exact jump-aheads (rfx::seq_add_n) from the
-// triangle setup: the scanline's edge values after j rows, then the span's
-// varyings after k pixels, then steps pixel by pixel like Iter::next.
+// K3b: scanline statistics and tile binning, one warp per triangle.
+// For every scanline of both halves (ScanlineIter::next, raster.rs:80-114)
+// the lane owning that row computes the exact edge values (closed-form run or
+// the general loop), then frags.i / oob as rasterize_fb counts them
+// (target.rs:259-264) and the pixel columns it covers; a warp reduction per
+// 32-row band gives the tiles to mark in the job's bitmask.
 // ---------------------------------------------------------------------------
 namespace {
 
-__device__ __forceinline__ uint32_t pack_px(uint32_t c, int32_t fmt) {
-    const uint32_t r = c & 0xFFu, g = (c >> 8) & 0xFFu, b = (c >> 16) & 0xFFu, a = c >> 24;
-    switch (fmt) {  // pixfmt.rs:76-103
-        case RF_K_ARGB8888: return (a << 24) | (r << 16) | (g << 8) | b;
-        case RF_K_XRGB8888: return (r << 16) | (g << 8) | b;
-        case RF_K_RGBA8888: return (r << 24) | (g << 16) | (b << 8) | a;
-        default: return (b << 24) | (g << 16) | (r << 8) | a;
-    }
-}
-
-__device__ __forceinline__ uint32_t to_color4(float r, float g, float b) {
-    // color.rs:253-263: (256 * c) as u8, alpha 0xFF.
-    return as_u8(fmul(256.0f, r)) | (as_u8(fmul(256.0f, g)) << 8) | (as_u8(fmul(256.0f, b)) << 16) |
-           0xFF000000u;
-}
-
-__device__ __forceinline__ uint32_t sample_tex(const DrawDev &d, float tu, float tv) {
-    const float w = (float)d.tw, h = (float)d.th;
-    uint32_t u, v;
-    if (d.sampler == RF_K_REPEAT_POT) {  // tex.rs:240-266
-        u = (uint32_t)as_i32(ffloor(fmul(w, tu))) & (d.tw - 1u);
-        v = (uint32_t)as_i32(ffloor(fmul(h, tv))) & (d.th - 1u);
-    } else if (d.sampler == RF_K_CLAMP) {  // tex.rs:272-304
-        float su = fmul(tu, w), sv = fmul(tv, h);
-        const float wm = fsub(w, 1.0f), hm = fsub(h, 1.0f);
-        su = su < 0.0f ? 0.0f : (su > wm ? wm : su);
-        sv = sv < 0.0f ? 0.0f : (sv > hm ? hm : sv);
-        u = as_u32(ffloor(su));
-        v = as_u32(ffloor(sv));
-    } else {  // SamplerOnce (tex.rs:313-357), index clamped instead of panicking
-        u = min(as_u32(fmul(w, tu)), d.tw - 1u);
-        v = min(as_u32(fmul(h, tv)), d.th - 1u);
-    }
-    return __ldg(d.tex + (size_t)v * d.tw + u);
-}
-
-template <int KIND>
-struct Kind {
-    static constexpr int NC = KIND == RF_K_FLAT ? 1
-                            : KIND == RF_K_TEXTURED ? 3
-                            : KIND == RF_K_TEX_GOURAUD ? 6 : 4;
-    __device__ static __forceinline__ uint32_t shade(const DrawDev &d, const float *v) {
-        if constexpr (KIND == RF_K_FLAT) {
-            return d.flat_rgba;
-        } else if constexpr (KIND == RF_K_GOURAUD) {
-            return to_color4(v[1], v[2], v[3]);
-        } else if constexpr (KIND == RF_K_TEXTURED) {
-            // Scanline::fragments: var.z_div(pos.z) (raster.rs:60-69)
-            return sample_tex(d, fdiv(v[1], v[0]), fdiv(v[2], v[0]));
-        } else if constexpr (KIND == RF_K_TEX_GOURAUD) {
-            const uint32_t t = sample_tex(d, fdiv(v[4], v[0]), fdiv(v[5], v[0]));
-            const float tr = fdiv((float)(t & 0xFFu), 256.0f);
-            const float tg = fdiv((float)((t >> 8) & 0xFFu), 256.0f);
-            const float tb = fdiv((float)((t >> 16) & 0xFFu), 256.0f);
-            return to_color4(fmul(tr, v[1]), fmul(tg, v[2]), fmul(tb, v[3]));
-        } else {  // GOURAUD_SRGB: Color3f<LinRgb>::to_srgb (color.rs:383-392)
-            const float ig = fdiv(1.0f, 2.2f);
-            return to_color4(powf(v[1], ig), powf(v[2], ig), powf(v[3], ig));
-        }
-    }
+struct RowOut {
+    unsigned long long frags_i;
+    uint32_t oob;
+    uint32_t px0, px1;  // covered pixel columns [px0, px1), px0 >= px1 if none
 };
 
-struct TileCtx {
-    uint32_t *scol;
-    float *sdep;
-    uint32_t lane;
-    uint32_t y;       // this lane's row
-    uint32_t tx0;     // first column of the tile
-    uint32_t ncols;   // columns of the tile inside the target
-    bool row_ok;
-    bool has_depth;
-    int32_t depth_test;
-    bool color_write, depth_write;
-    int32_t fmt;
-    uint32_t w;
-    unsigned long long frags_o;
-};
-
-// One scanline segment: the lane's row j of half h, clipped to the tile.
-template <int KIND>
-__device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec &h, uint32_t j) {
-    constexpr int NC = Kind<KIND>::NC;
-    const float lx = seq_add_n(h.lx, h.dlx, j);
-    const float rx = seq_add_n(h.rx, h.drx, j);
+// Scanline j of half H landing on row y (< h).
+__device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_t j, uint32_t w,
+                                          RowOut &o) {
+    const float lx = row_value(H, RF_R_LX, j);
+    const float rx = row_value(H, RF_R_RX, j);
     const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
     const uint64_t xs = as_usize(x0r);
     uint64_t xe = as_usize(x1r);
     if (xe < xs) xe = xs;
-    if (xs >= T.tx0 + T.ncols) return;
+    o.frags_i += xe - xs;
+    if (xe > w) o.oob += 1;
     uint64_t nfr = xe - xs;
     const uint32_t cnt = as_u32(fsub(x1r, x0r));
     if (cnt < nfr) nfr = cnt;
-    const uint64_t send = xs + nfr;  // xs < 2^32 here, no overflow
-    const uint32_t a = (uint32_t)(xs > T.tx0 ? xs : T.tx0);
-    const uint32_t b = (uint32_t)(send < (uint64_t)(T.tx0 + T.ncols) ? send : (uint64_t)(T.tx0 + T.ncols));
-    if (a >= b) return;
-    // v0 = left.next(); v0 = v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:88-102)
-    const float tshift = fsub(x0r, lx);
-    const uint32_t k0 = a - (uint32_t)xs;
-    float v[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-        const float c0 = seq_add_n(h.c[c], h.dc[c], j);
-        const float adj = fadd(c0, fmul(fsub(fadd(c0, h.dvdx[c]), c0), tshift));
-        v[c] = seq_add_n(adj, h.dvdx[c], k0);
-    }
-    float dv[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) dv[c] = h.dvdx[c];
-    uint32_t idx = (a - T.tx0) * RF_TILE_H + T.lane;
-    for (uint32_t x = a; x < b; ++x, idx += RF_TILE_H) {
-        const float z = v[0];
-        bool pass = true;
-        if (T.has_depth) {
-            const float cur = T.sdep[idx];
-            switch (T.depth_test) {  // ctx.rs:86-89
-                case RF_K_DEPTH_NONE: pass = true; break;
-                case RF_K_DEPTH_LESS: pass = cur < z; break;
-                case RF_K_DEPTH_EQUAL: pass = cur == z; break;
-                default: pass = cur > z; break;
-            }
-        }
-        if (pass) {
-            if (T.color_write) {
-                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
-                T.frags_o += 1;
-            }
-            if (T.has_depth && T.depth_write) T.sdep[idx] = z;
-        }
-#pragma unroll
-        for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
-    }
-}
-
-template <int KIND>
-__device__ __forceinline__ void raster_half(TileCtx &T, const DrawDev &d, const HalfRec &h) {
-    if (h.n == 0 || !T.row_ok) return;
-    if (!(fabsf(h.y0r) < RF_MAX_COORD)) return;
-    // Row of scanline j is (y0r + j) as usize = max(0, Y + j), Y = y0r - 0.5.
-    const int32_t Y = (int32_t)fsub(h.y0r, 0.5f);
-    if (T.y > 0 || Y >= 0) {
-        const int64_t j = (int64_t)T.y - Y;
-        if (j >= 0 && j < (int64_t)h.n) span<KIND>(T, d, h, (uint32_t)j);
-    } else {
-        const int64_t jn = min((int64_t)h.n, (int64_t)1 - Y);
-        for (int64_t j = 0; j < jn; ++j) span<KIND>(T, d, h, (uint32_t)j);
-    }
-}
-
-__device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restrict__ draws,
-                                            const PrimRec *__restrict__ P) {
-    if (!P->live) return;
-    const DrawDev &d = draws[P->draw];
-    const HalfRec h0 = P->half[0];
-    const HalfRec h1 = P->half[1];
-    switch (d.shader) {
-        case RF_K_FLAT: raster_half<RF_K_FLAT>(T, d, h0); raster_half<RF_K_FLAT>(T, d, h1); break;
-        case RF_K_GOURAUD: raster_half<RF_K_GOURAUD>(T, d, h0); raster_half<RF_K_GOURAUD>(T, d, h1); break;
-        case RF_K_TEXTURED: raster_half<RF_K_TEXTURED>(T, d, h0); raster_half<RF_K_TEXTURED>(T, d, h1); break;
-        case RF_K_TEX_GOURAUD:
-            raster_half<RF_K_TEX_GOURAUD>(T, d, h0);
-            raster_half<RF_K_TEX_GOURAUD>(T, d, h1);
-            break;
-        default:
-            raster_half<RF_K_GOURAUD_SRGB>(T, d, h0);
-            raster_half<RF_K_GOURAUD_SRGB>(T, d, h1);
-            break;
+    if (nfr && xs < w) {
+        o.px0 = min(o.px0, (uint32_t)xs);
+        o.px1 = max(o.px1, (uint32_t)(xs + nfr < w ? xs + nfr : w));
     }
 }
 
 }  // namespace
 
-template <int TW>
-__global__ void __launch_bounds__(RF_RASTER_MAX_THREADS)
-k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict__ draws,
-         const PrimRec *__restrict__ prims, const uint32_t *__restrict__ tcnt,
-         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ mask,
-         uint32_t ntiles_total, uint32_t *__restrict__ tile_queue, StatsDev *__restrict__ stats) {
-    extern __shared__ uint32_t smem[];
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *scol = smem + warp * (2 * TW * RF_TILE_H);
-    float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
-    for (;;) {
-        uint32_t tile = 0;
-        if (lane == 0) tile = atomicAdd(tile_queue, 1u);
-        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
-        if (tile >= ntiles_total) break;
-        const uint32_t ji = upper_index(nj, tile, [&](uint32_t i) { return jobs[i].tile_base; });
-        const JobDev &J = jobs[ji];
-        const uint32_t lt = tile - J.tile_base;
-        const uint32_t tyi = lt / J.tiles_x, txi = lt - tyi * J.tiles_x;
-        TileCtx T;
-        T.scol = scol;
-        T.sdep = sdep;
-        T.lane = lane;
-        T.tx0 = txi * TW;
-        T.y = tyi * RF_TILE_H + lane;
-        T.ncols = min((uint32_t)TW, J.w - T.tx0);
-        T.row_ok = T.y < J.h;
-        T.has_depth = J.depth != nullptr;
-        T.depth_test = J.depth_test;
-        T.color_write = J.color_write != 0;
-        T.depth_write = J.depth_write != 0;
-        T.fmt = J.pixfmt;
-        T.w = J.w;
-        T.frags_o = 0;
-        const size_t row_off = (size_t)T.y * J.w + T.tx0;
-        bool loaded = false;
-        auto load_tile = [&]() {
-            // Lane r loads row r; colour/depth come from the target or from
-            // a pending clear (the clear is fused into this load).
-            for (uint32_t x = 0; x < (uint32_t)TW; ++x) {
-                const uint32_t i = x * RF_TILE_H + lane;
-                const bool in = T.row_ok && x < T.ncols;
-                scol[i] = (J.clear_flags & 1u) ? J.clear_px : (in ? J.color[row_off + x] : 0u);
-                if (T.has_depth)
-                    sdep[i] = (J.clear_flags & 2u) ? J.clear_z : (in ? J.depth[row_off + x] : 0.0f);
+__global__ void k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
+                      const PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev,
+                      uint32_t tile_w, uint32_t *__restrict__ mask, StatsDev *__restrict__ stats) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t np = *nprims_dev;
+    uint32_t cur_job = 0xFFFFFFFFu;
+    unsigned long long acc_fi = 0, acc_oob = 0;  // per-lane, for cur_job
+    auto flush = [&]() {
+        if (cur_job != 0xFFFFFFFFu) {
+            warp_add_u64(&stats[cur_job].frags_i, acc_fi, true);
+            warp_add_u64(&stats[cur_job].oob, acc_oob, true);
+        }
+        acc_fi = acc_oob = 0;
+    };
+    for (uint32_t p = wid; p < np; p += nw) {
+        const PrimRec *P = prims + p;
+        if (!P->live) continue;
+        const uint32_t job = draws[P->draw].job;
+        if (job != cur_job) {
+            flush();
+            cur_job = job;
+        }
+        const JobDev &J = jobs[job];
+        const uint32_t tl = P->tri - J.tri_base;
+        const uint32_t word = tl >> 5, bit = 1u << (tl & 31);
+        for (int hh = 0; hh < 2; ++hh) {
+            const HalfRec *H = &P->half[hh];
+            const uint32_t n = H->n;
+            if (n == 0) continue;
+            const float y0r = H->y0r;
+            if (!(fabsf(y0r) < RF_MAX_COORD)) {  // outside the supported range
+                if (lane == 0) acc_oob += 1;
+                continue;
             }
-        };
-        const uint32_t *tmask = mask + J.mask_base + (size_t)lt * J.mask_words;
-        for (uint32_t wb = 0; wb < J.mask_words; wb += 32) {
-            const uint32_t word = wb + lane < J.mask_words ? tmask[wb + lane] : 0u;
-            uint32_t bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
-            if (bal && !loaded) {
-                load_tile();
-                loaded = true;
+            const int64_t Y = (int64_t)fsub(y0r, 0.5f);  // row(j) = max(0, Y + j)
+            const int64_t hh64 = (int64_t)J.h;
+            // Scanlines at or below the buffer's last row count only in oob.
+            const int64_t in_rows = min((int64_t)n, max((int64_t)0, hh64 - Y));
+            if (lane == 0) acc_oob += (unsigned long long)((int64_t)n - in_rows);
+            if (in_rows <= 0) continue;
+            // Rows above the buffer all land on row 0: walked by lane 0.
+            RowOut o0{0, 0, 0xFFFFFFFFu, 0};
+            int64_t jfirst = 0;
+            if (Y < 0) {
+                jfirst = min(in_rows, (int64_t)1 - Y);
+                if (lane == 0)
+                    for (int64_t j = 0; j < jfirst; ++j) row_stats(H, (uint32_t)j, J.w, o0);
             }
-            while (bal) {
-                const uint32_t src = __ffs(bal) - 1;
-                bal &= bal - 1;
-                uint32_t wv = __shfl_sync(0xFFFFFFFFu, word, src);
-                while (wv) {
-                    const uint32_t b = __ffs(wv) - 1;
-                    wv &= wv - 1;
-                    const uint32_t gt = J.tri_base + (wb + src) * 32 + b;
-                    const uint32_t p0 = toff[gt], pc = tcnt[gt];
-                    for (uint32_t p = p0; p < p0 + pc; ++p) raster_prim(T, draws, prims + p);
+            // Remaining rows y = Y + j > 0 (or all rows when Y >= 0), by band.
+            const int64_t ylo = Y + jfirst, yhi = Y + in_rows - 1;
+            for (int64_t band = (ylo > 0 ? ylo : 0) / RF_TILE_H; band * RF_TILE_H <= yhi; ++band) {
+                const int64_t y = band * RF_TILE_H + lane;
+                RowOut o{0, 0, 0xFFFFFFFFu, 0};
+                if (y >= ylo && y <= yhi) row_stats(H, (uint32_t)(y - Y), J.w, o);
+                if (band == 0) {  // fold the rows above the buffer into band 0
+                    o.frags_i += o0.frags_i;
+                    o.oob += o0.oob;
+                    o.px0 = min(o.px0, o0.px0);
+                    o.px1 = max(o.px1, o0.px1);
+                    o0 = RowOut{0, 0, 0xFFFFFFFFu, 0};
+                }
+                acc_fi += o.frags_i;
+                acc_oob += o.oob;
+                uint32_t lo = o.px0 < o.px1 ? o.px0 : 0xFFFFFFFFu, hi = o.px0 < o.px1 ? o.px1 : 0u;
+#pragma unroll
+                for (int s = 16; s > 0; s >>= 1) {
+                    lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, s));
+                    hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, s));
+                }
+                if (lo < hi) {
+                    const uint32_t t0 = lo / tile_w, t1 = (hi - 1) / tile_w;
+                    uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
+                    for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
+                }
+            }
+            // Band 0 not visited (no row y > 0): flush the row-0 walk of
+            // lane 0.  The test is made warp-uniform before the shuffles.
+            const bool pend0 = __shfl_sync(0xFFFFFFFFu, (o0.frags_i || o0.oob || o0.px0 < o0.px1) ? 1 : 0, 0) != 0;
+            if (pend0) {
+                acc_fi += o0.frags_i;
+                acc_oob += o0.oob;
+                uint32_t lo = __shfl_sync(0xFFFFFFFFu, o0.px0, 0), hi = __shfl_sync(0xFFFFFFFFu, o0.px1, 0);
+                if (lo < hi) {
+                    const uint32_t t0 = lo / tile_w, t1 = (hi - 1) / tile_w;
+                    uint32_t *row = mask + J.mask_base + word;
+                    for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
                 }
             }
         }
-        if (!loaded && J.clear_flags) {
-            load_tile();
-            loaded = true;
-        }
-        if (loaded && T.row_ok) {
-            for (uint32_t x = 0; x < T.ncols; ++x) {
-                const uint32_t i = x * RF_TILE_H + lane;
-                J.color[row_off + x] = scol[i];
-                if (T.has_depth) J.depth[row_off + x] = sdep[i];
-            }
-        }
-        __syncwarp();
-        const uint32_t j0 = __shfl_sync(0xFFFFFFFFu, ji, 0);
-        warp_add_u64(&stats[j0].frags_o, T.frags_o, true);
     }
+    flush();
 }
 
 // Frame::clear applied directly (when no render follows before a read).
@@ -838,48 +635,30 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, uint32_t *mask, StatsDev *stats, int nsm, cudaStream_t s) {
+                         PrimRec *prims, const uint32_t *nprims_dev, uint32_t *mask,
+                         StatsDev *stats, int nsm, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
     uint32_t blocks = min((nt + 127) / 128, (uint32_t)nsm * 16);
-    k_setup<<<blocks, 128, 0, s>>>(draws, nd, jobs, nt, tile_w, cpos, tcnt, toff, tpoly, pool,
-                                   prims, mask, stats);
+    k_setup<<<blocks, 128, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool, prims, stats);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // one warp per output triangle; the count is only known on the device
+    uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
+    k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, nprims_dev, tile_w, mask, stats);
     return cudaGetLastError();
 }
 
-template <int TW>
-static cudaError_t launch_raster_tw(const JobDev *jobs, uint32_t nj, const DrawDev *draws,
-                                    const PrimRec *prims, const uint32_t *tcnt,
-                                    const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
-                                    uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
-                                    cudaStream_t s) {
-    const size_t smem = (size_t)warps * 2 * TW * RF_TILE_H * 4;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_raster<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster<TW>, warps * 32, smem);
-    if (per_sm < 1) per_sm = 1;
-    uint32_t blocks = (uint32_t)per_sm * (uint32_t)nsm;
-    const uint32_t need = (ntiles + warps - 1) / warps;
-    if (blocks > need) blocks = need;
-    if (blocks == 0) blocks = 1;
-    k_raster<TW><<<blocks, warps * 32, smem, s>>>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles,
-                                                 queue, stats);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_raster(uint32_t tile_w, const JobDev *jobs, uint32_t nj, const DrawDev *draws,
-                          const PrimRec *prims, const uint32_t *tcnt, const uint32_t *toff,
-                          const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
-                          StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
+cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,
+                          const DrawDev *draws, const PrimRec *prims, const uint32_t *tcnt,
+                          const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
+                          uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
+                          cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     switch (tile_w) {
-        case 8: return launch_raster_tw<8>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        case 16: return launch_raster_tw<16>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        case 64: return launch_raster_tw<64>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        default: return launch_raster_tw<32>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 8: return launch_raster_tw8(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 16: return launch_raster_tw16(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 64: return launch_raster_tw64(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        default: return launch_raster_tw32(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
     }
 }
 

@@ -14,6 +14,7 @@
 #define RF_K_TEXTURED 2
 #define RF_K_TEX_GOURAUD 3
 #define RF_K_GOURAUD_SRGB 4
+#define RF_K_ANY 5  // rasteriser kernel that dispatches on each triangle's kind
 #define RF_K_REPEAT_POT 0
 #define RF_K_CLAMP 1
 #define RF_K_ONCE 2
@@ -53,14 +54,31 @@ cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const fl
 size_t scan_scratch_words(uint32_t n);
 cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch,
                         uint32_t *total, cudaStream_t s);
+// Triangle setup (k_setup) followed by scanline statistics and tile binning
+// (k_bin); nprims_dev = the device-side total of output triangles.
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, uint32_t *mask, StatsDev *stats, int nsm, cudaStream_t s);
-cudaError_t launch_raster(uint32_t tile_w, const JobDev *jobs, uint32_t nj, const DrawDev *draws,
-                          const PrimRec *prims, const uint32_t *tcnt, const uint32_t *toff,
-                          const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
-                          StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s);
+                         PrimRec *prims, const uint32_t *nprims_dev, uint32_t *mask,
+                         StatsDev *stats, int nsm, cudaStream_t s);
+// kind: the shader kind shared by every draw of the jobs, or RF_K_ANY;
+// fast: every job uses the default context on a target with depth.
+cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,
+                          const DrawDev *draws, const PrimRec *prims, const uint32_t *tcnt,
+                          const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
+                          uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
+                          cudaStream_t s);
+#define RF_DECL_RASTER_TW(TW)                                                                  \
+    cudaError_t launch_raster_tw##TW(int kind, bool fast, const JobDev *jobs, uint32_t nj,      \
+                                     const DrawDev *draws, const PrimRec *prims,                \
+                                     const uint32_t *tcnt, const uint32_t *toff,                \
+                                     const uint32_t *mask, uint32_t ntiles, uint32_t *queue,    \
+                                     StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s);
+RF_DECL_RASTER_TW(8)
+RF_DECL_RASTER_TW(16)
+RF_DECL_RASTER_TW(32)
+RF_DECL_RASTER_TW(64)
+#undef RF_DECL_RASTER_TW
 cudaError_t launch_fill(uint32_t *color, float *depth, size_t n, uint32_t px, float z,
                         uint32_t flags, int nsm, cudaStream_t s);
 }  // namespace rfk

@@ -9,7 +9,7 @@
 // the scratch space from a fixed area compiled into it.
 //
 // The scratch is one file-scope __device__ array of RF_NOALLOC_SCRATCH_BYTES
-// (about 2 MB).  Every GPU that loads the library keeps that area until the
+// (8 MiB).  Every GPU that loads the library keeps that area until the
 // process exits.  Host code only sees a host-side stand-in for the array's
 // name, so the device address is looked up with cudaGetSymbolAddress, once
 // per device, with that device current, on the first call made on it.  That
@@ -211,8 +211,10 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
                                cnt, nsm, s));
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
-                                mask, sd, nsm, s));
-        NA_CK(rfk::launch_raster(TILE_W, jd, 1, dd, prims, tcnt, toff, mask, ntiles,
+                                cnt + RF_CNT_PRIMS, mask, sd, nsm, s));
+        const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
+                          flags->depth_write;
+        NA_CK(rfk::launch_raster(TILE_W, shader, fast, jd, 1, dd, prims, tcnt, toff, mask, ntiles,
                                  cnt + RF_CNT_QUEUE, sd, WARPS, nsm, s));
     }
     if (stats) {

@@ -1,0 +1,514 @@
+// rf_raster.cuh — the tile rasteriser (k_raster), included by one
+// translation unit per tile width (rf_raster_tw*.cu) so the specialised
+// kernels compile in parallel.
+#ifndef RF_RASTER_CUH
+#define RF_RASTER_CUH
+
+#include <cuda_runtime.h>
+
+#include "rf_device.cuh"
+
+// ---------------------------------------------------------------------------
+// K4: tile rasteriser.
+// A warp owns one tile of RF_TILE_H rows x TW columns at a time; lane r owns
+// row r of the tile for the whole tile, so per-pixel submission order is the
+// order in which the lane walks the triangle list — no atomics, no sorting.
+// Colour and depth sit in shared memory column-major (word x*32 + r): the
+// bank of every access is the lane id, whatever x each lane is at.
+// Each lane enters its row with exact jump-aheads (rfx::seq_add_n) from the
+// triangle setup: the scanline's edge values after j rows, then the span's
+// varyings after k pixels, then steps pixel by pixel like Iter::next.
+// ---------------------------------------------------------------------------
+namespace rfr {
+using namespace rfx;
+using namespace rfd;
+
+__device__ __forceinline__ uint32_t pack_px(uint32_t c, int32_t fmt) {
+    const uint32_t r = c & 0xFFu, g = (c >> 8) & 0xFFu, b = (c >> 16) & 0xFFu, a = c >> 24;
+    switch (fmt) {  // pixfmt.rs:76-103
+        case RF_K_ARGB8888: return (a << 24) | (r << 16) | (g << 8) | b;
+        case RF_K_XRGB8888: return (r << 16) | (g << 8) | b;
+        case RF_K_RGBA8888: return (r << 24) | (g << 16) | (b << 8) | a;
+        default: return (b << 24) | (g << 16) | (r << 8) | a;
+    }
+}
+
+__device__ __forceinline__ uint32_t to_color4(float r, float g, float b) {
+    // color.rs:253-263: (256 * c) as u8, alpha 0xFF.
+    return as_u8(fmul(256.0f, r)) | (as_u8(fmul(256.0f, g)) << 8) | (as_u8(fmul(256.0f, b)) << 16) |
+           0xFF000000u;
+}
+
+__device__ __forceinline__ uint32_t sample_tex(const DrawDev &d, float tu, float tv) {
+    const float w = (float)d.tw, h = (float)d.th;
+    uint32_t u, v;
+    if (d.sampler == RF_K_REPEAT_POT) {  // tex.rs:240-266
+        u = (uint32_t)as_i32(ffloor(fmul(w, tu))) & (d.tw - 1u);
+        v = (uint32_t)as_i32(ffloor(fmul(h, tv))) & (d.th - 1u);
+    } else if (d.sampler == RF_K_CLAMP) {  // tex.rs:272-304
+        float su = fmul(tu, w), sv = fmul(tv, h);
+        const float wm = fsub(w, 1.0f), hm = fsub(h, 1.0f);
+        su = su < 0.0f ? 0.0f : (su > wm ? wm : su);
+        sv = sv < 0.0f ? 0.0f : (sv > hm ? hm : sv);
+        u = as_u32(ffloor(su));
+        v = as_u32(ffloor(sv));
+    } else {  // SamplerOnce (tex.rs:313-357), index clamped instead of panicking
+        u = min(as_u32(fmul(w, tu)), d.tw - 1u);
+        v = min(as_u32(fmul(h, tv)), d.th - 1u);
+    }
+    return __ldg(d.tex + (size_t)v * d.tw + u);
+}
+
+template <int KIND>
+struct Kind {
+    static constexpr int NC = KIND == RF_K_FLAT ? 1
+                            : KIND == RF_K_TEXTURED ? 3
+                            : KIND == RF_K_TEX_GOURAUD ? 6 : 4;
+    __device__ static __forceinline__ uint32_t shade(const DrawDev &d, const float *v) {
+        if constexpr (KIND == RF_K_FLAT) {
+            return d.flat_rgba;
+        } else if constexpr (KIND == RF_K_GOURAUD) {
+            return to_color4(v[1], v[2], v[3]);
+        } else if constexpr (KIND == RF_K_TEXTURED) {
+            // Scanline::fragments: var.z_div(pos.z) (raster.rs:60-69)
+            return sample_tex(d, fdiv(v[1], v[0]), fdiv(v[2], v[0]));
+        } else if constexpr (KIND == RF_K_TEX_GOURAUD) {
+            const uint32_t t = sample_tex(d, fdiv(v[4], v[0]), fdiv(v[5], v[0]));
+            const float tr = fdiv((float)(t & 0xFFu), 256.0f);
+            const float tg = fdiv((float)((t >> 8) & 0xFFu), 256.0f);
+            const float tb = fdiv((float)((t >> 16) & 0xFFu), 256.0f);
+            return to_color4(fmul(tr, v[1]), fmul(tg, v[2]), fmul(tb, v[3]));
+        } else {  // GOURAUD_SRGB: Color3f<LinRgb>::to_srgb (color.rs:383-392)
+            const float ig = fdiv(1.0f, 2.2f);
+            return to_color4(powf(v[1], ig), powf(v[2], ig), powf(v[3], ig));
+        }
+    }
+};
+
+struct TileCtx {
+    uint32_t *scol;
+    float *sdep;
+    uint32_t lane;
+    uint32_t y;       // this lane's row
+    uint32_t tx0;     // first column of the tile
+    uint32_t tx1;     // one past the last column of the tile inside the target
+    bool row_ok;
+    bool has_depth;
+    int32_t depth_test;
+    bool color_write, depth_write;
+    int32_t fmt;
+    unsigned long long frags_o;
+};
+
+// The lane's scanline j of half H (raster.rs:84-113), clipped to the tile,
+// then its fragments (raster.rs:60-69) into the tile (target.rs:163-198).
+// FAST: the default context (depth test Less, colour and depth writes on).
+template <int KIND, bool FAST>
+__device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec *__restrict__ H,
+                                     uint32_t j) {
+    constexpr int NC = Kind<KIND>::NC;
+    const float lx = row_value(H, RF_R_LX, j);
+    const float rx = row_value(H, RF_R_RX, j);
+    const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
+    const uint64_t xs = as_usize(x0r);
+    uint64_t xe = as_usize(x1r);
+    if (xe < xs) xe = xs;
+    if (xs >= T.tx1) return;
+    uint64_t nfr = xe - xs;
+    const uint32_t cnt = as_u32(fsub(x1r, x0r));
+    if (cnt < nfr) nfr = cnt;
+    const uint64_t send = xs + nfr;  // xs < 2^32 here, no overflow
+    const uint32_t a = (uint32_t)(xs > T.tx0 ? xs : T.tx0);
+    const uint32_t b = (uint32_t)(send < (uint64_t)T.tx1 ? send : (uint64_t)T.tx1);
+    if (a >= b) return;
+    // v0 = left.next(); v0 = v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:88-102),
+    // then k0 pixel steps to the tile's first column.
+    const float tshift = fsub(x0r, lx);
+    const uint32_t k0 = a - (uint32_t)xs;
+    float v[NC], dv[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        dv[c] = H->dvdx[c];
+        const float c0 = row_value(H, RF_R_C + c, j);
+        const float adj = fadd(c0, fmul(fsub(fadd(c0, dv[c]), c0), tshift));
+        v[c] = jump(adj, dv[c], k0);
+    }
+    uint32_t idx = (a - T.tx0) * RF_TILE_H + T.lane;
+    const uint32_t end = (b - T.tx0) * RF_TILE_H + T.lane;
+    if (FAST) {
+        // Two pixels per iteration: their depth tests and shading are
+        // independent; only the running sums chain from pixel to pixel.
+        uint32_t nout = 0;
+        for (; idx + RF_TILE_H < end; idx += 2 * RF_TILE_H) {
+            float v1[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v1[c] = fadd(v[c], dv[c]);
+            const float c0 = T.sdep[idx], c1 = T.sdep[idx + RF_TILE_H];
+            const float z0 = v[0], z1 = v1[0];
+            if (c0 < z0) {  // ctx.rs:86-89 with Some(Less)
+                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                T.sdep[idx] = z0;
+                ++nout;
+            }
+            if (c1 < z1) {
+                T.scol[idx + RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
+                T.sdep[idx + RF_TILE_H] = z1;
+                ++nout;
+            }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = fadd(v1[c], dv[c]);
+        }
+        if (idx != end) {
+            const float z = v[0];
+            if (T.sdep[idx] < z) {
+                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                T.sdep[idx] = z;
+                ++nout;
+            }
+        }
+        T.frags_o += nout;
+        return;
+    }
+    for (; idx != end; idx += RF_TILE_H) {
+        const float z = v[0];
+        bool pass = true;
+        if (T.has_depth) {
+            const float cur = T.sdep[idx];
+            switch (T.depth_test) {  // ctx.rs:86-89
+                case RF_K_DEPTH_NONE: pass = true; break;
+                case RF_K_DEPTH_LESS: pass = cur < z; break;
+                case RF_K_DEPTH_EQUAL: pass = cur == z; break;
+                default: pass = cur > z; break;
+            }
+        }
+        if (pass) {
+            if (T.color_write) {
+                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                T.frags_o += 1;
+            }
+            if (T.has_depth && T.depth_write) T.sdep[idx] = z;
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
+    }
+}
+
+// Which scanline of a half lands on row y: row(j) = (y0r + j) as usize =
+// max(0, Y + j) with Y = y0r - 1/2.  Returns the j range [j0, j1) for row y
+// (one scanline for rows below the top edge; row 0 also collects the rows
+// above the buffer).
+__device__ __forceinline__ void rows_for(const HalfRec *__restrict__ H, uint32_t y, uint32_t &j0,
+                                         uint32_t &j1) {
+    j0 = j1 = 0;
+    const uint32_t n = H->n;
+    const float y0r = H->y0r;
+    if (n == 0 || !(fabsf(y0r) < RF_MAX_COORD)) return;
+    const int32_t Y = (int32_t)fsub(y0r, 0.5f);
+    if (y > 0 || Y >= 0) {
+        const int64_t j = (int64_t)y - Y;
+        if (j >= 0 && j < (int64_t)n) {
+            j0 = (uint32_t)j;
+            j1 = j0 + 1;
+        }
+    } else {
+        j1 = (uint32_t)min((int64_t)n, (int64_t)1 - Y);
+    }
+}
+
+template <int KIND, bool FAST>
+__device__ __forceinline__ void raster_prim_k(TileCtx &T, const DrawDev &d, const PrimRec *__restrict__ P) {
+    if (!T.row_ok) return;
+    // The two halves cover disjoint rows, so each lane walks only the half
+    // holding its row and both halves run in one pass of the warp.  Only
+    // row 0 can take scanlines of both halves (rows above the buffer).
+    uint32_t a0, a1, b0, b1;
+    rows_for(&P->half[0], T.y, a0, a1);
+    rows_for(&P->half[1], T.y, b0, b1);
+    const bool start1 = a1 == a0;
+    const HalfRec *H = start1 ? &P->half[1] : &P->half[0];
+    uint32_t j = start1 ? b0 : a0, jend = start1 ? b1 : a1;
+    bool more = !start1 && b1 > b0;
+    for (;;) {
+        if (j >= jend) {
+            if (!more) break;
+            H = &P->half[1];
+            j = b0;
+            jend = b1;
+            more = false;
+            continue;
+        }
+        span<KIND, FAST>(T, d, H, j);
+        ++j;
+    }
+}
+
+// KIND: the shader kind of every draw of the job, or RF_K_ANY (dispatch per
+// triangle).
+template <int KIND, bool FAST>
+__device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restrict__ draws,
+                                            const PrimRec *__restrict__ P) {
+    if (!P->live) return;
+    const DrawDev &d = draws[P->draw];
+    if (KIND != RF_K_ANY) {
+        raster_prim_k<KIND == RF_K_ANY ? 0 : KIND, FAST>(T, d, P);
+        return;
+    }
+    switch (P->kind) {
+        case RF_K_FLAT: raster_prim_k<RF_K_FLAT, FAST>(T, d, P); break;
+        case RF_K_GOURAUD: raster_prim_k<RF_K_GOURAUD, FAST>(T, d, P); break;
+        case RF_K_TEXTURED: raster_prim_k<RF_K_TEXTURED, FAST>(T, d, P); break;
+        case RF_K_TEX_GOURAUD: raster_prim_k<RF_K_TEX_GOURAUD, FAST>(T, d, P); break;
+        default: raster_prim_k<RF_K_GOURAUD_SRGB, FAST>(T, d, P); break;
+    }
+}
+
+// Walks a tile's bitmask in submission order: set bits of the mask words
+// (input triangles), each expanded to its clipped output triangles.
+// Warp-uniform state; every lane calls next() together.
+struct PrimIter {
+    const uint32_t *tmask;
+    const uint32_t *toff;
+    const uint32_t *tcnt;
+    uint32_t nwords, tri_base, lane;
+    uint32_t wb, word, bal, src, wv, p, pend;
+    bool started;
+    __device__ __forceinline__ uint32_t next() {
+        for (;;) {
+            if (p < pend) return p++;
+            if (wv) {
+                const uint32_t b = __ffs(wv) - 1;
+                wv &= wv - 1;
+                const uint32_t gt = tri_base + (wb + src) * 32 + b;
+                p = toff[gt];
+                pend = p + tcnt[gt];
+                continue;
+            }
+            if (bal) {
+                src = __ffs(bal) - 1;
+                bal &= bal - 1;
+                wv = __shfl_sync(0xFFFFFFFFu, word, src);
+                continue;
+            }
+            if (started) wb += 32;
+            started = true;
+            if (wb >= nwords) return 0xFFFFFFFFu;
+            word = wb + lane < nwords ? tmask[wb + lane] : 0u;
+            bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
+        }
+    }
+};
+
+// Asynchronous copy of one triangle record into this warp's staging slot
+// (16 bytes per lane; one commit group per call on every lane).
+__device__ __forceinline__ void stage_prim(PrimRec *slot, const PrimRec *src, uint32_t lane) {
+    static_assert(sizeof(PrimRec) % 16 == 0, "PrimRec must be a whole number of 16-byte chunks");
+    static_assert(sizeof(PrimRec) <= 64 * 16, "PrimRec is staged in at most two rounds");
+    constexpr uint32_t CHUNKS = sizeof(PrimRec) / 16;
+    if (src) {
+#pragma unroll
+        for (uint32_t c = lane; c < CHUNKS; c += 32) {
+            const uint32_t sa = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char *>(slot) + c * 16);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+                         "l"(reinterpret_cast<const char *>(src) + c * 16)
+                         : "memory");
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void wait_staged_but_one() {
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    __syncwarp();
+}
+
+}  // namespace rfr
+
+// KIND: shader kind of every draw of the job (or RF_K_ANY); FAST: the
+// default context (depth test Less, colour and depth writes) on a target
+// with depth.
+template <int TW, int KIND, bool FAST>
+__global__ void __launch_bounds__(RF_RASTER_MAX_THREADS)
+k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict__ draws,
+         const PrimRec *__restrict__ prims, const uint32_t *__restrict__ tcnt,
+         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ mask,
+         uint32_t ntiles_total, uint32_t *__restrict__ tile_queue, StatsDev *__restrict__ stats) {
+    using namespace rfr;
+    extern __shared__ __align__(16) uint32_t smem[];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr uint32_t WARP_WORDS = 2 * TW * RF_TILE_H + 2 * (sizeof(PrimRec) / 4);
+    uint32_t *scol = smem + warp * WARP_WORDS;
+    float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
+    PrimRec *stage = reinterpret_cast<PrimRec *>(scol + 2 * TW * RF_TILE_H);
+    for (;;) {
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(tile_queue, 1u);
+        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
+        if (tile >= ntiles_total) break;
+        const uint32_t ji = upper_index(nj, tile, [&](uint32_t i) { return jobs[i].tile_base; });
+        const JobDev &J = jobs[ji];
+        const uint32_t lt = tile - J.tile_base;
+        const uint32_t tyi = lt / J.tiles_x, txi = lt - tyi * J.tiles_x;
+        TileCtx T;
+        T.scol = scol;
+        T.sdep = sdep;
+        T.lane = lane;
+        T.tx0 = txi * TW;
+        T.tx1 = min(T.tx0 + (uint32_t)TW, J.w);
+        T.y = tyi * RF_TILE_H + lane;
+        T.row_ok = T.y < J.h;
+        T.has_depth = J.depth != nullptr;
+        T.depth_test = J.depth_test;
+        T.color_write = J.color_write != 0;
+        T.depth_write = J.depth_write != 0;
+        T.fmt = J.pixfmt;
+        T.frags_o = 0;
+        const uint32_t ncols = T.tx1 - T.tx0;
+        const size_t row_off = (size_t)T.y * J.w + T.tx0;
+        // Lane r moves row r; 16-byte vectors when the row start is aligned.
+        const bool vec = ((J.w | T.tx0) & 3u) == 0u && ncols == (uint32_t)TW &&
+                         (((uintptr_t)J.color | (uintptr_t)J.depth) & 15u) == 0u;
+        bool loaded = false;
+        auto load_tile = [&]() {
+            const bool cc = J.clear_flags & 1u, cd = (J.clear_flags & 2u) != 0u;
+            if (vec && T.row_ok && !(cc && cd)) {
+                for (uint32_t x = 0; x < (uint32_t)TW; x += 4) {
+                    uint4 c4 = cc ? make_uint4(J.clear_px, J.clear_px, J.clear_px, J.clear_px)
+                                  : *reinterpret_cast<const uint4 *>(J.color + row_off + x);
+                    scol[(x + 0) * RF_TILE_H + lane] = c4.x;
+                    scol[(x + 1) * RF_TILE_H + lane] = c4.y;
+                    scol[(x + 2) * RF_TILE_H + lane] = c4.z;
+                    scol[(x + 3) * RF_TILE_H + lane] = c4.w;
+                    if (T.has_depth) {
+                        float4 d4 = cd ? make_float4(J.clear_z, J.clear_z, J.clear_z, J.clear_z)
+                                       : *reinterpret_cast<const float4 *>(J.depth + row_off + x);
+                        sdep[(x + 0) * RF_TILE_H + lane] = d4.x;
+                        sdep[(x + 1) * RF_TILE_H + lane] = d4.y;
+                        sdep[(x + 2) * RF_TILE_H + lane] = d4.z;
+                        sdep[(x + 3) * RF_TILE_H + lane] = d4.w;
+                    }
+                }
+            } else {
+                for (uint32_t x = 0; x < (uint32_t)TW; ++x) {
+                    const uint32_t i = x * RF_TILE_H + lane;
+                    const bool in = T.row_ok && x < ncols;
+                    scol[i] = cc ? J.clear_px : (in ? J.color[row_off + x] : 0u);
+                    if (T.has_depth) sdep[i] = cd ? J.clear_z : (in ? J.depth[row_off + x] : 0.0f);
+                }
+            }
+        };
+        PrimIter it;
+        it.tmask = mask + J.mask_base + (size_t)lt * J.mask_words;
+        it.toff = toff;
+        it.tcnt = tcnt;
+        it.nwords = J.mask_words;
+        it.tri_base = J.tri_base;
+        it.lane = lane;
+        it.wb = it.word = it.bal = it.src = it.wv = it.p = it.pend = 0;
+        it.started = false;
+        // Double-buffered: the record of the next triangle is in flight
+        // while the current one is rasterised.
+        uint32_t cur = it.next();
+        if (cur != 0xFFFFFFFFu) {
+            load_tile();
+            loaded = true;
+            stage_prim(stage + 0, prims + cur, lane);
+            uint32_t nxt = it.next();
+            stage_prim(stage + 1, nxt != 0xFFFFFFFFu ? prims + nxt : nullptr, lane);
+            uint32_t slot = 0;
+            for (;;) {
+                wait_staged_but_one();
+                raster_prim<KIND, FAST>(T, draws, stage + slot);
+                __syncwarp();
+                if (nxt == 0xFFFFFFFFu) break;
+                const uint32_t after = it.next();
+                stage_prim(stage + slot, after != 0xFFFFFFFFu ? prims + after : nullptr, lane);
+                slot ^= 1u;
+                nxt = after;
+            }
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+        }
+        if (!loaded && J.clear_flags) {
+            load_tile();
+            loaded = true;
+        }
+        if (loaded && T.row_ok) {
+            if (vec) {
+                for (uint32_t x = 0; x < (uint32_t)TW; x += 4) {
+                    *reinterpret_cast<uint4 *>(J.color + row_off + x) =
+                        make_uint4(scol[(x + 0) * RF_TILE_H + lane], scol[(x + 1) * RF_TILE_H + lane],
+                                   scol[(x + 2) * RF_TILE_H + lane], scol[(x + 3) * RF_TILE_H + lane]);
+                    if (T.has_depth)
+                        *reinterpret_cast<float4 *>(J.depth + row_off + x) =
+                            make_float4(sdep[(x + 0) * RF_TILE_H + lane], sdep[(x + 1) * RF_TILE_H + lane],
+                                        sdep[(x + 2) * RF_TILE_H + lane], sdep[(x + 3) * RF_TILE_H + lane]);
+                }
+            } else {
+                for (uint32_t x = 0; x < ncols; ++x) {
+                    const uint32_t i = x * RF_TILE_H + lane;
+                    J.color[row_off + x] = scol[i];
+                    if (T.has_depth) J.depth[row_off + x] = sdep[i];
+                }
+            }
+        }
+        __syncwarp();
+        const uint32_t j0 = __shfl_sync(0xFFFFFFFFu, ji, 0);
+        warp_add_u64(&stats[j0].frags_o, T.frags_o, true);
+    }
+}
+
+namespace rfk {
+
+template <int TW, int KIND, bool FAST>
+static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDev *draws,
+                                   const PrimRec *prims, const uint32_t *tcnt,
+                                   const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
+                                   uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
+                                   cudaStream_t s) {
+    const size_t smem = (size_t)warps * (2 * TW * RF_TILE_H * 4 + 2 * sizeof(PrimRec));
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_raster<TW, KIND, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster<TW, KIND, FAST>, warps * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    uint32_t blocks = (uint32_t)per_sm * (uint32_t)nsm;
+    const uint32_t need = (ntiles + warps - 1) / warps;
+    if (blocks > need) blocks = need;
+    if (blocks == 0) blocks = 1;
+    k_raster<TW, KIND, FAST><<<blocks, warps * 32, smem, s>>>(jobs, nj, draws, prims, tcnt, toff, mask,
+                                                       ntiles, queue, stats);
+    return cudaGetLastError();
+}
+
+// Launcher for one tile width: picks the kernel specialised for the job's
+// shader kind and context (fast = the default context on a depth target;
+// any other context runs the generic kernel).
+template <int TW>
+static cudaError_t launch_raster_for_width(int kind, bool fast, const JobDev *jobs, uint32_t nj,
+                                           const DrawDev *draws, const PrimRec *prims,
+                                           const uint32_t *tcnt, const uint32_t *toff,
+                                           const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
+                                           StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
+    if (!fast)
+        return launch_raster_k<TW, RF_K_ANY, false>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+    switch (kind) {
+        case RF_K_FLAT:
+            return launch_raster_k<TW, RF_K_FLAT, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case RF_K_GOURAUD:
+            return launch_raster_k<TW, RF_K_GOURAUD, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case RF_K_TEXTURED:
+            return launch_raster_k<TW, RF_K_TEXTURED, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case RF_K_TEX_GOURAUD:
+            return launch_raster_k<TW, RF_K_TEX_GOURAUD, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case RF_K_GOURAUD_SRGB:
+            return launch_raster_k<TW, RF_K_GOURAUD_SRGB, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        default:
+            return launch_raster_k<TW, RF_K_ANY, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+    }
+}
+
+}  // namespace rfk
+
+#endif

@@ -25,6 +25,8 @@ def shim(tmp_path_factory):
     L.shim_check.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
                              C.POINTER(C.c_uint64)]
     L.shim_check.restype = C.c_uint64
+    L.shim_check_fast.argtypes = L.shim_check.argtypes
+    L.shim_check_fast.restype = C.c_uint64
     return L
 
 
@@ -32,11 +34,13 @@ def _check(L, s, d, k):
     s = np.ascontiguousarray(s, np.float32)
     d = np.ascontiguousarray(d, np.float32)
     k = np.ascontiguousarray(k, np.uint32)
-    fb = C.c_uint64(0)
-    bad = L.shim_check(s.ctypes.data, d.ctypes.data, k.ctypes.data, s.size, C.byref(fb))
-    if bad:
-        i = fb.value
-        pytest.fail("%d mismatches; first s=%r d=%r k=%d" % (bad, s[i], d[i], k[i]))
+    for fn in (L.shim_check, L.shim_check_fast):
+        fb = C.c_uint64(0)
+        bad = fn(s.ctypes.data, d.ctypes.data, k.ctypes.data, s.size, C.byref(fb))
+        if bad:
+            i = fb.value
+            pytest.fail("%s: %d mismatches; first s=%r d=%r k=%d"
+                        % (fn.__name__, bad, s[i], d[i], k[i]))
 
 
 def test_vary_kats(shim):
