@@ -144,7 +144,8 @@ rf_status rf_texture_upload(rf_ctx *ctx, const uint32_t *rgba, uint32_t w, uint3
 rf_status rf_texture_destroy(rf_ctx *ctx, rf_texture tex);
 /* Framebuf<Colorbuf<Buf2<u32>, pixfmt>, Buf2<f32>> (target.rs:35-44) when
  * has_depth, else a colour-only Colorbuf (target.rs:138-161).  Contents
- * start zeroed, like Buf2::new (buf.rs:155-161). */
+ * start zeroed, like Buf2::new (buf.rs:155-161).  w, h <= RF_MAX_TARGET_DIM. */
+#define RF_MAX_TARGET_DIM 32768u
 rf_status rf_target_create(rf_ctx *ctx, uint32_t w, uint32_t h, int32_t pixfmt,
                            int32_t has_depth, rf_target *out);
 rf_status rf_target_destroy(rf_ctx *ctx, rf_target t);

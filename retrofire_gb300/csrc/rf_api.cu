@@ -6,6 +6,7 @@
 // (core/src/render.rs:134-207) and the draws of a job are rendered in order.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -57,6 +58,13 @@ struct rf_ctx {
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
+    DevBuf triw, trib, scan64, rowtot, rows, rprims;
+    // Row-record capacity (words): grown when a frame asked for more, which
+    // the library learns from an asynchronous read-back of the total.
+    uint64_t rows_cap = 0;
+    unsigned long long *rows_need_host = nullptr;  // pinned
+    cudaEvent_t rows_evt = nullptr;
+    bool rows_evt_pending = false;
     // stats: host-side counts + device-accumulated counts, and what was
     // already handed out by rf_ctx_take_stats / rf_render
     rf_stats host_acc{};
@@ -252,6 +260,23 @@ rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const floa
     if ((st = ensure(ctx, ctx->prims, (size_t)nt * RF_MAX_FAN * sizeof(PrimRec)))) return st;
     if ((st = ensure(ctx, ctx->mask, mask_words * 4))) return st;
     if ((st = ensure(ctx, ctx->scan, rfk::scan_scratch_words((uint32_t)nt) * 4))) return st;
+    if ((st = ensure(ctx, ctx->triw, nt * 4))) return st;
+    if ((st = ensure(ctx, ctx->trib, nt * 8))) return st;
+    if ((st = ensure(ctx, ctx->scan64, rfk::scan64_scratch_words((uint32_t)nt) * 8))) return st;
+    if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
+    if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
+    if (!ctx->rows_need_host) {
+        CK(cudaMallocHost(&ctx->rows_need_host, sizeof(unsigned long long)));
+        CK(cudaEventCreateWithFlags(&ctx->rows_evt, cudaEventDisableTiming));
+    }
+    if (ctx->rows_evt_pending && cudaEventQuery(ctx->rows_evt) == cudaSuccess) {
+        const uint64_t need = *ctx->rows_need_host;
+        if (need > ctx->rows_cap) ctx->rows_cap = need + need / 4;
+        ctx->rows_evt_pending = false;
+    }
+    if (ctx->rows_cap == 0) ctx->rows_cap = std::max<uint64_t>((uint64_t)nt * 160u, 1u << 22);
+    if (ctx->rows_cap > 0xFFFF0000ull) ctx->rows_cap = 0xFFFF0000ull;  // 32-bit record offsets
+    if ((st = ensure(ctx, ctx->rows, ctx->rows_cap * 4))) return st;
 
     cudaStream_t s = ctx->stream;
     std::vector<cudaEvent_t> ev;
@@ -291,14 +316,23 @@ rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const floa
     CK(mark(RF_STAGE_SETUP));
     CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
                          P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
-                         P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), counters + RF_CNT_PRIMS, P<uint32_t>(ctx->mask),
-                         P<StatsDev>(ctx->stats), ctx->nsm, s));
+                         P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), counters + RF_CNT_PRIMS,
+                         P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
+                         P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
+                         P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
+                         P<uint32_t>(ctx->mask), P<StatsDev>(ctx->stats), counters, ctx->nsm, s));
+    if (!ctx->rows_evt_pending) {
+        CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(ctx->rows_evt, s));
+        ctx->rows_evt_pending = true;
+    }
     CK(mark(RF_STAGE_RASTER));
     int kind = hd[0].shader;
     for (const DrawDev &d : hd)
         if (d.shader != kind) kind = RF_K_ANY;
     const bool fast = tg.depth && fl->depth_test == RF_DEPTH_LESS && fl->color_write && fl->depth_write;
-    CK(rfk::launch_raster(TW, kind, fast, jd, 1, dd, P<PrimRec>(ctx->prims), P<uint32_t>(ctx->tcnt),
+    CK(rfk::launch_raster(TW, kind, fast, jd, 1, dd, P<PrimRec>(ctx->prims),
+                          P<RasterPrim>(ctx->rprims), P<uint32_t>(ctx->rows), P<uint32_t>(ctx->tcnt),
                           P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles,
                           counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->warps, ctx->nsm, s));
     CK(mark(RF_STAGE_N));
@@ -389,7 +423,10 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); }
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
-                      &ctx->counters, &ctx->stats};
+                      &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
+                      &ctx->rowtot, &ctx->rows, &ctx->rprims};
+    if (ctx->rows_need_host) cudaFreeHost(ctx->rows_need_host);
+    if (ctx->rows_evt) cudaEventDestroy(ctx->rows_evt);
     for (DevBuf *b : bufs) cudaFree(b->p);
     for (auto &ev : ctx->ev_pending)
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
@@ -528,7 +565,7 @@ rf_status rf_texture_destroy(rf_ctx *ctx, rf_texture tex) {
 
 rf_status rf_target_create(rf_ctx *ctx, uint32_t w, uint32_t h, int32_t pixfmt, int32_t has_depth,
                            rf_target *out) {
-    if (!ctx || !out || !w || !h || w > 65536 || h > 65536) return RF_ERR_BAD_ARG;
+    if (!ctx || !out || !w || !h || w > RF_MAX_TARGET_DIM || h > RF_MAX_TARGET_DIM) return RF_ERR_BAD_ARG;
     if (pixfmt < RF_ARGB8888 || pixfmt > RF_BGRA8888) return RF_ERR_BAD_ARG;
     Target t;
     t.w = w;

@@ -90,10 +90,16 @@ RF_HD uint64_t as_usize(float x) {
     if (x >= 18446744073709551616.0f) return UINT64_MAX;
     return (uint64_t)x;
 }
+RF_HD uint32_t as_u32(float x);
+// as_usize with the 64-bit conversion only for values that need it.
+RF_HD uint64_t as_usize_fast(float x);
 RF_HD uint32_t as_u32(float x) {
     if (!(x > 0.0f)) return 0;
     if (x >= 4294967296.0f) return UINT32_MAX;
     return (uint32_t)x;
+}
+RF_HD uint64_t as_usize_fast(float x) {
+    return x < 4294967296.0f ? (uint64_t)as_u32(x) : as_usize(x);
 }
 RF_HD int32_t as_i32(float x) {
     if (x != x) return 0;
@@ -298,37 +304,63 @@ RF_HD void fast_params(float s, float d, int32_t &dinc, uint32_t &kmax) {
 
 // k sequential additions with the single-binade run tried inline first and
 // the general loop out of line (it is rarely needed).
-RF_HD float jump(float s, float d, uint32_t k) {
-    if (k == 0u) return s;
+//
+// run_try: one run of k steps from s inside its binade; on success returns
+// true with the result in out.  Otherwise returns false with n = the steps
+// that do stay inside the binade (n < k; 0 when none or when s is not a
+// normal number above the first binade, d not normal, or a tie).
+RF_HD bool run_try(float s, float d, uint32_t k, float &out, uint32_t &n) {
+    n = 0;
     const uint32_t sb = f2u(s), db = f2u(d);
     const uint32_t se = (sb >> 23) & 0xFFu, de = (db >> 23) & 0xFFu;
-    if (se - 2u < 253u && de - 1u < 254u) {  // s normal above the first binade, d normal
-        const uint32_t m = (sb & 0x7FFFFFu) | 0x800000u;
-        const uint32_t md = (db & 0x7FFFFFu) | 0x800000u;
-        const int32_t sh = (int32_t)se - (int32_t)de;
-        if (sh >= -7) {
-            uint32_t inc = 0;
-            bool ok = true;
-            if (sh <= 0) {
-                inc = md << (uint32_t)(-sh);
-            } else if (sh < 25) {
-                const uint32_t q = md >> (uint32_t)sh;
-                const uint32_t rem = md & ((1u << (uint32_t)sh) - 1u);
-                const uint32_t half = 1u << (uint32_t)(sh - 1);
-                ok = rem != half;  // ties take the general path
-                inc = q + (rem > half ? 1u : 0u);
-            }
-            if (ok) {
-                const uint64_t total = (uint64_t)inc * (uint64_t)k;
-                if (((sb ^ db) >> 31) == 0u) {
-                    if ((uint64_t)m + total <= 0xFFFFFFull) return u2f(sb + (uint32_t)total);
-                } else if ((uint64_t)m >= total + 0x800001ull) {
-                    return u2f(sb - (uint32_t)total);
-                }
-            }
-        }
+    if (!(se - 2u < 253u && de - 1u < 254u)) return false;
+    const uint32_t m = (sb & 0x7FFFFFu) | 0x800000u;
+    const uint32_t md = (db & 0x7FFFFFu) | 0x800000u;
+    const int32_t sh = (int32_t)se - (int32_t)de;
+    if (sh < -7) return false;
+    uint32_t inc = 0;
+    if (sh <= 0) {
+        inc = md << (uint32_t)(-sh);
+    } else if (sh < 25) {
+        const uint32_t q = md >> (uint32_t)sh;
+        const uint32_t rem = md & ((1u << (uint32_t)sh) - 1u);
+        const uint32_t half = 1u << (uint32_t)(sh - 1);
+        if (rem == half) return false;  // ties take the general path
+        inc = q + (rem > half ? 1u : 0u);
     }
-    return seq_add_n(s, d, k);
+    if (inc == 0u) return false;
+    const uint64_t total = (uint64_t)inc * (uint64_t)k;
+    if (((sb ^ db) >> 31) == 0u) {
+        if ((uint64_t)m + total <= 0xFFFFFFull) {
+            out = u2f(sb + (uint32_t)total);
+            return true;
+        }
+        n = udiv24(0xFFFFFFu - m, inc);
+    } else {
+        if ((uint64_t)m >= total + 0x800001ull) {
+            out = u2f(sb - (uint32_t)total);
+            return true;
+        }
+        n = m >= 0x800001u ? udiv24(m - 0x800001u, inc) : 0u;
+    }
+    out = u2f(((sb ^ db) >> 31) == 0u ? sb + n * inc : sb - n * inc);
+    return false;
+}
+
+// Inline: one run, or one run to the binade edge, the explicit edge step
+// and a second run; anything else goes to the general loop.
+RF_HD float jump(float s, float d, uint32_t k) {
+    if (k == 0u) return s;
+    float r;
+    uint32_t n;
+    if (run_try(s, d, k, r, n)) return r;
+    if (n == 0u) return seq_add_n(s, d, k);
+    const float t = fadd(r, d);  // the step across the edge
+    const uint32_t k2 = k - n - 1u;
+    if (k2 == 0u) return t;
+    uint32_t n2;
+    if (run_try(t, d, k2, r, n2)) return r;
+    return seq_add_n(t, d, k2);
 }
 
 }  // namespace rfx

@@ -290,6 +290,91 @@ __global__ void k_scan_add(uint32_t *__restrict__ out, uint32_t n, const uint32_
         if (base + i < n) out[base + i] += add;
 }
 
+// Exclusive scan of u32 values into u64 (row-record offsets).
+__global__ void k_scan64_blocks(const uint32_t *__restrict__ in, unsigned long long *__restrict__ out,
+                                uint32_t n, unsigned long long *__restrict__ block_sums) {
+    __shared__ unsigned long long warp_sums[32];
+    const uint32_t base = blockIdx.x * (SCAN_THREADS * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
+    unsigned long long v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = base + i < n ? in[base + i] : 0u;
+        s += v[i];
+    }
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long ws = warp_sums[lane], wi = ws;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if (lane >= (uint32_t)o) wi += y;
+        }
+        warp_sums[lane] = wi - ws;
+        if (lane == 31) block_sums[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    unsigned long long run = warp_sums[wid] + incl - s;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) out[base + i] = run;
+        run += v[i];
+    }
+}
+
+__global__ void k_scan64_sums(unsigned long long *__restrict__ sums, uint32_t nb,
+                              unsigned long long *__restrict__ total) {
+    __shared__ unsigned long long warp_sums[32];
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < nb; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const unsigned long long s = i < nb ? sums[i] : 0u;
+        unsigned long long incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31) warp_sums[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            unsigned long long ws = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0u, wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+                if (lane >= (uint32_t)o) wi += y;
+            }
+            warp_sums[lane] = wi - ws;
+        }
+        __syncthreads();
+        const unsigned long long excl = carry + warp_sums[wid] + incl - s;
+        if (i < nb) sums[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + s;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan64_add(unsigned long long *__restrict__ out, uint32_t n,
+                             const unsigned long long *__restrict__ sums) {
+    const uint32_t base = blockIdx.x * (SCAN_THREADS * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
+    const unsigned long long add = sums[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i)
+        if (base + i < n) out[base + i] += add;
+}
+
 // ---------------------------------------------------------------------------
 // K3: triangle setup.
 // ---------------------------------------------------------------------------
@@ -353,12 +438,18 @@ __device__ void scan_setup(float y0, float y1, const SV &l0, const SV &l1, const
 
 }  // namespace
 
-__global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
+#define RF_SETUP_THREADS 64
+__global__ void __launch_bounds__(RF_SETUP_THREADS)
+k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const JobDev *__restrict__ jobs, uint32_t nt_total,
                         const float4 *__restrict__ cpos, const uint32_t *__restrict__ tcnt,
                         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ tpoly,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
-                        StatsDev *__restrict__ stats) {
+                        uint32_t *__restrict__ tri_words, StatsDev *__restrict__ stats) {
+    // Each thread builds its record in shared memory; the warp then writes
+    // the records out with coalesced 16-byte stores.
+    __shared__ __align__(16) PrimRec srec[RF_SETUP_THREADS];
+    const uint32_t lane = threadIdx.x & 31, wbase = threadIdx.x & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < nt_total; base += stride) {
         const uint32_t gt = base + threadIdx.x;
@@ -366,18 +457,24 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
         const uint32_t cnt = active ? tcnt[gt] : 0u;
         uint32_t job = 0xFFFFFFFFu;
         unsigned long long prims_o = 0;
+        uint32_t di = 0, t = 0, nc = 0, na = 0, zm = 0, slot = RF_NO_POLY, p0 = 0;
         if (cnt) {
-            const uint32_t di = upper_index(nd, gt, [&](uint32_t i) { return draws[i].tri_base; });
-            const DrawDev &d = draws[di];
-            job = d.job;
-            const JobDev &J = jobs[job];
-            const uint32_t t = gt - d.tri_base;
-            const uint32_t nc = 1 + nattr_of(d.shader);
-            const uint32_t na = nc - 1;
-            const uint32_t zm = zdiv_mask_of(d.shader);
-            const uint32_t slot = tpoly[gt];
-            const uint32_t p0 = toff[gt];
-            for (uint32_t c = 0; c < cnt; ++c) {
+            di = upper_index(nd, gt, [&](uint32_t i) { return draws[i].tri_base; });
+            job = draws[di].job;
+            t = gt - draws[di].tri_base;
+            nc = 1 + nattr_of(draws[di].shader);
+            na = nc - 1;
+            zm = zdiv_mask_of(draws[di].shader);
+            slot = tpoly[gt];
+            p0 = toff[gt];
+        }
+        const uint32_t maxc = __reduce_max_sync(0xFFFFFFFFu, cnt);
+        uint32_t words = 0;  // row-record words of this input triangle so far
+        for (uint32_t c = 0; c < maxc; ++c) {
+            const bool have = c < cnt;
+            if (have) {
+                const DrawDev &d = draws[di];
+                const JobDev &J = jobs[job];
                 // Gather the three clip-space vertices of this (fan) triangle.
                 float pos[3][4], at[3][RF_MAX_ATTR];
                 for (int k = 0; k < 3; ++k) {
@@ -412,12 +509,14 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 const bool backface = wz < 0.0f;
                 const bool culled = (J.face_cull == RF_K_CULL_BACK && backface) ||
                                     (J.face_cull == RF_K_CULL_FRONT && !backface);
-                PrimRec &P = prims[p0 + c];
+                PrimRec &P = srec[threadIdx.x];
                 P.draw = di;
                 P.live = culled ? 0u : 1u;
                 P.tri = gt;
                 P.kind = d.shader;
-                if (culled) continue;
+                P.rloc = words;
+                P.rwords = 0;
+                if (!culled) {
                 prims_o += 1;
                 // raster.rs:185-224 tri_fill: stable sort by y (total_cmp).
                 SV v0 = sv[0], v1 = sv[1], v2 = sv[2], tmp;
@@ -432,13 +531,43 @@ __global__ void k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 const bool mid0_left = v1.x < mid1.x;
                 const SV &left = mid0_left ? v1 : mid1;
                 const SV &right = mid0_left ? mid1 : v1;
-                HalfRec h0, h1;
-                scan_setup(v0.y, v1.y, v0, left, v0, right, nc, h0);
-                scan_setup(v1.y, v2.y, left, v2, right, v2, nc, h1);
-                P.half[0] = h0;
-                P.half[1] = h1;
+                scan_setup(v0.y, v1.y, v0, left, v0, right, nc, P.half[0]);
+                scan_setup(v1.y, v2.y, left, v2, right, v2, nc, P.half[1]);
+                // Row records for the scanlines that land on the target's
+                // rows, unless a half starts above the buffer (its rows map
+                // onto row 0 several times: rasterised from this record).
+                uint32_t rows = 0;
+                bool regular = true;
+                for (int hh = 0; hh < 2; ++hh) {
+                    const HalfRec &H = P.half[hh];
+                    if (H.n == 0 || !(fabsf(H.y0r) < RF_MAX_COORD)) continue;
+                    const int32_t Y = (int32_t)fsub(H.y0r, 0.5f);
+                    if (Y < 0) regular = false;
+                    const int64_t in = min((int64_t)H.n, max((int64_t)0, (int64_t)J.h - Y));
+                    rows += (uint32_t)in;
+                }
+                const uint64_t w = regular ? (uint64_t)rows * (1u + nc) : 0u;
+                if (w < 0x40000000ull && (uint64_t)words + w < 0x40000000ull) {
+                    P.rwords = (uint32_t)w;
+                    words += (uint32_t)w;
+                }
+                }
             }
+            __syncwarp();
+            // Write out the records built in this round, one per pass.
+            uint32_t bal = __ballot_sync(0xFFFFFFFFu, have);
+            const uint32_t dst = p0 + c;
+            while (bal) {
+                const uint32_t l = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const uint32_t dl = __shfl_sync(0xFFFFFFFFu, dst, l);
+                const uint4 *src = reinterpret_cast<const uint4 *>(&srec[wbase + l]);
+                uint4 *out = reinterpret_cast<uint4 *>(prims + dl);
+                for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) out[q] = src[q];
+            }
+            __syncwarp();
         }
+        if (active) tri_words[gt] = words;
         // Stats, aggregated per warp when all lanes share one job.
         const uint32_t hasjob = __ballot_sync(0xFFFFFFFFu, job != 0xFFFFFFFFu);
         if (hasjob) {
@@ -475,8 +604,8 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_
     const float lx = row_value(H, RF_R_LX, j);
     const float rx = row_value(H, RF_R_RX, j);
     const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-    const uint64_t xs = as_usize(x0r);
-    uint64_t xe = as_usize(x1r);
+    const uint64_t xs = as_usize_fast(x0r);
+    uint64_t xe = as_usize_fast(x1r);
     if (xe < xs) xe = xs;
     o.frags_i += xe - xs;
     if (xe > w) o.oob += 1;
@@ -491,13 +620,22 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_
 
 }  // namespace
 
-__global__ void k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
-                      const PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev,
-                      uint32_t tile_w, uint32_t *__restrict__ mask, StatsDev *__restrict__ stats) {
-    const uint32_t lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256)
+k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
+      const PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev, uint32_t tile_w,
+      const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
+      unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
+      StatsDev *__restrict__ stats, uint32_t *__restrict__ counters) {
+    const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t np = *nprims_dev;
+    __shared__ __align__(16) PrimRec srec[8];  // one per warp of the 256-thread block
+    __shared__ __align__(16) RasterPrim srp[8];
+    __shared__ float stab[8][32][RF_NR + 1];   // scanline values of one band
+    PrimRec *sP = &srec[wib];
+    RasterPrim *R = &srp[wib];
+    float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
     unsigned long long acc_fi = 0, acc_oob = 0;  // per-lane, for cur_job
     auto flush = [&]() {
@@ -507,80 +645,182 @@ __global__ void k_bin(const DrawDev *__restrict__ draws, const JobDev *__restric
         }
         acc_fi = acc_oob = 0;
     };
-    for (uint32_t p = wid; p < np; p += nw) {
-        const PrimRec *P = prims + p;
-        if (!P->live) continue;
-        const uint32_t job = draws[P->draw].job;
-        if (job != cur_job) {
-            flush();
-            cur_job = job;
-        }
-        const JobDev &J = jobs[job];
-        const uint32_t tl = P->tri - J.tri_base;
-        const uint32_t word = tl >> 5, bit = 1u << (tl & 31);
-        for (int hh = 0; hh < 2; ++hh) {
-            const HalfRec *H = &P->half[hh];
-            const uint32_t n = H->n;
-            if (n == 0) continue;
-            const float y0r = H->y0r;
-            if (!(fabsf(y0r) < RF_MAX_COORD)) {  // outside the supported range
-                if (lane == 0) acc_oob += 1;
-                continue;
-            }
-            const int64_t Y = (int64_t)fsub(y0r, 0.5f);  // row(j) = max(0, Y + j)
-            const int64_t hh64 = (int64_t)J.h;
-            // Scanlines at or below the buffer's last row count only in oob.
-            const int64_t in_rows = min((int64_t)n, max((int64_t)0, hh64 - Y));
-            if (lane == 0) acc_oob += (unsigned long long)((int64_t)n - in_rows);
-            if (in_rows <= 0) continue;
-            // Rows above the buffer all land on row 0: walked by lane 0.
-            RowOut o0{0, 0, 0xFFFFFFFFu, 0};
-            int64_t jfirst = 0;
-            if (Y < 0) {
-                jfirst = min(in_rows, (int64_t)1 - Y);
-                if (lane == 0)
-                    for (int64_t j = 0; j < jfirst; ++j) row_stats(H, (uint32_t)j, J.w, o0);
-            }
-            // Remaining rows y = Y + j > 0 (or all rows when Y >= 0), by band.
-            const int64_t ylo = Y + jfirst, yhi = Y + in_rows - 1;
-            for (int64_t band = (ylo > 0 ? ylo : 0) / RF_TILE_H; band * RF_TILE_H <= yhi; ++band) {
-                const int64_t y = band * RF_TILE_H + lane;
-                RowOut o{0, 0, 0xFFFFFFFFu, 0};
-                if (y >= ylo && y <= yhi) row_stats(H, (uint32_t)(y - Y), J.w, o);
-                if (band == 0) {  // fold the rows above the buffer into band 0
-                    o.frags_i += o0.frags_i;
-                    o.oob += o0.oob;
-                    o.px0 = min(o.px0, o0.px0);
-                    o.px1 = max(o.px1, o0.px1);
-                    o0 = RowOut{0, 0, 0xFFFFFFFFu, 0};
-                }
-                acc_fi += o.frags_i;
-                acc_oob += o.oob;
-                uint32_t lo = o.px0 < o.px1 ? o.px0 : 0xFFFFFFFFu, hi = o.px0 < o.px1 ? o.px1 : 0u;
+    // One band of the target: reduce the lanes' covered columns and mark the
+    // band's tiles with this triangle's bit.
+    auto mark_band = [&](int64_t band, RowOut &o, const JobDev &J, uint32_t word, uint32_t bit) {
+        uint32_t lo = o.px0 < o.px1 ? o.px0 : 0xFFFFFFFFu, hi = o.px0 < o.px1 ? o.px1 : 0u;
 #pragma unroll
-                for (int s = 16; s > 0; s >>= 1) {
-                    lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, s));
-                    hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, s));
-                }
-                if (lo < hi) {
-                    const uint32_t t0 = lo / tile_w, t1 = (hi - 1) / tile_w;
-                    uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
-                    for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
+        for (int sft = 16; sft > 0; sft >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, sft));
+            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, sft));
+        }
+        if (lo < hi) {
+            const uint32_t t0 = lo / tile_w, t1 = (hi - 1) / tile_w;
+            uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
+            for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
+        }
+    };
+    for (uint32_t p = wid; p < np; p += nw) {
+        __syncwarp();
+        {
+            const uint4 *src = reinterpret_cast<const uint4 *>(prims + p);
+            uint4 *dst = reinterpret_cast<uint4 *>(sP);
+            for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) dst[q] = src[q];
+        }
+        if (lane == 0) {
+            R->draw = sP->draw;
+            R->flags = sP->live ? RF_RP_LIVE : 0u;
+            R->kind = sP->kind;
+            R->base = 0;
+            R->stride = 0;
+            R->y0 = R->c0 = R->y1 = R->c1 = 0;
+        }
+        __syncwarp();
+        const PrimRec *P = sP;
+        if (P->live) {
+            const uint32_t job = draws[P->draw].job;
+            if (job != cur_job) {
+                flush();
+                cur_job = job;
+            }
+            const JobDev &J = jobs[job];
+            const uint32_t tl = P->tri - J.tri_base;
+            const uint32_t word = tl >> 5, bit = 1u << (tl & 31);
+            const uint32_t nc = 1 + nattr_of(P->kind);
+            const uint32_t nr = RF_R_C + nc;
+            const uint32_t stride = 1 + nc;
+            bool regular = P->rwords != 0;
+            unsigned long long base = 0;
+            if (regular) {
+                base = tri_wbase[P->tri] + P->rloc;
+                if (base + P->rwords > rows_cap) {  // no room: rasterise from the PrimRec
+                    regular = false;
+                    if (lane == 0) atomicAdd(&counters[RF_CNT_ROWSOVF], 1u);
                 }
             }
-            // Band 0 not visited (no row y > 0): flush the row-0 walk of
-            // lane 0.  The test is made warp-uniform before the shuffles.
-            const bool pend0 = __shfl_sync(0xFFFFFFFFu, (o0.frags_i || o0.oob || o0.px0 < o0.px1) ? 1 : 0, 0) != 0;
-            if (pend0) {
-                acc_fi += o0.frags_i;
-                acc_oob += o0.oob;
-                uint32_t lo = __shfl_sync(0xFFFFFFFFu, o0.px0, 0), hi = __shfl_sync(0xFFFFFFFFu, o0.px1, 0);
-                if (lo < hi) {
-                    const uint32_t t0 = lo / tile_w, t1 = (hi - 1) / tile_w;
-                    uint32_t *row = mask + J.mask_base + word;
-                    for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
+            if (lane == 0 && regular) {
+                R->flags |= RF_RP_ROWS;
+                R->base = (uint32_t)base;
+                R->stride = stride;
+            }
+            uint32_t rec_off = 0;
+            for (int hh = 0; hh < 2; ++hh) {
+                const HalfRec *H = &P->half[hh];
+                const uint32_t n = H->n;
+                if (lane < RF_NC) R->dvdx[hh][lane] = H->dvdx[lane];
+                if (n == 0) continue;
+                const float y0r = H->y0r;
+                if (!(fabsf(y0r) < RF_MAX_COORD)) {  // outside the supported range
+                    if (lane == 0) acc_oob += 1;
+                    continue;
+                }
+                const int64_t Y = (int64_t)fsub(y0r, 0.5f);  // row(j) = max(0, Y + j)
+                // Scanlines at or below the buffer's last row count only in oob.
+                const int64_t in_rows = min((int64_t)n, max((int64_t)0, (int64_t)J.h - Y));
+                if (lane == 0) acc_oob += (unsigned long long)((int64_t)n - in_rows);
+                if (in_rows <= 0) continue;
+                if (regular) {
+                    // Scanlines y = Y + j: walked sequentially, one lane per
+                    // row quantity (ScanlineIter::next's running sums), then
+                    // one lane per row for the span, stats and row record.
+                    if (lane == 0) {
+                        if (hh == 0) { R->y0 = (uint32_t)Y; R->c0 = (uint32_t)in_rows; }
+                        else { R->y1 = (uint32_t)Y; R->c1 = (uint32_t)in_rows; }
+                    }
+                    float wv = lane < nr ? u2f(H->b0[lane]) : 0.0f;
+                    const float wd = lane < nr ? H->d[lane] : 0.0f;
+                    const int64_t ylo = Y, yhi = Y + in_rows - 1;
+                    for (int64_t band = ylo / RF_TILE_H; band * RF_TILE_H <= yhi; ++band) {
+                        const int64_t ys = max(ylo, band * RF_TILE_H);
+                        const int64_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
+                        if (lane < nr) {
+                            const uint32_t m = (uint32_t)(ye - ys + 1);
+                            for (uint32_t i = 0; i < m; ++i) {
+                                T[i][lane] = wv;
+                                wv = fadd(wv, wd);
+                            }
+                        }
+                        __syncwarp();
+                        const int64_t y = band * RF_TILE_H + lane;
+                        RowOut o{0, 0, 0xFFFFFFFFu, 0};
+                        if (y >= ys && y <= ye) {
+                            const uint32_t i = (uint32_t)(y - ys);
+                            const float lx = T[i][RF_R_LX], rx = T[i][RF_R_RX];
+                            const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
+                            const uint64_t xs = as_usize_fast(x0r);
+                            uint64_t xe = as_usize_fast(x1r);
+                            if (xe < xs) xe = xs;
+                            o.frags_i = xe - xs;
+                            if (xe > J.w) o.oob = 1;
+                            uint64_t nfr = xe - xs;
+                            const uint32_t cnt = as_u32(fsub(x1r, x0r));
+                            if (cnt < nfr) nfr = cnt;
+                            uint32_t w0 = 0;
+                            if (nfr && xs < J.w) {
+                                o.px0 = (uint32_t)xs;
+                                o.px1 = (uint32_t)(xs + nfr < J.w ? xs + nfr : J.w);
+                                w0 = o.px0 | (o.px1 << 16);
+                            }
+                            uint32_t *rec = rows + base + (size_t)(rec_off + (uint32_t)(y - Y)) * stride;
+                            rec[0] = w0;
+                            // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102)
+                            const float tshift = fsub(x0r, lx);
+                            for (uint32_t c = 0; c < nc; ++c) {
+                                const float cv = T[i][RF_R_C + c], dv = H->dvdx[c];
+                                rec[1 + c] = f2u(fadd(cv, fmul(fsub(fadd(cv, dv), cv), tshift)));
+                            }
+                        }
+                        acc_fi += o.frags_i;
+                        acc_oob += o.oob;
+                        mark_band(band, o, J, word, bit);
+                        __syncwarp();
+                    }
+                    rec_off += (uint32_t)in_rows;
+                    continue;
+                }
+                // Rows above the buffer all land on row 0: walked by lane 0.
+                RowOut o0{0, 0, 0xFFFFFFFFu, 0};
+                int64_t jfirst = 0;
+                if (Y < 0) {
+                    jfirst = min(in_rows, (int64_t)1 - Y);
+                    if (lane == 0)
+                        for (int64_t j = 0; j < jfirst; ++j) row_stats(H, (uint32_t)j, J.w, o0);
+                }
+                // Remaining rows y = Y + j > 0 (or all rows when Y >= 0), by band.
+                const int64_t ylo = Y + jfirst, yhi = Y + in_rows - 1;
+                for (int64_t band = (ylo > 0 ? ylo : 0) / RF_TILE_H; band * RF_TILE_H <= yhi; ++band) {
+                    const int64_t y = band * RF_TILE_H + lane;
+                    RowOut o{0, 0, 0xFFFFFFFFu, 0};
+                    if (y >= ylo && y <= yhi) row_stats(H, (uint32_t)(y - Y), J.w, o);
+                    if (band == 0) {  // fold the rows above the buffer into band 0
+                        o.frags_i += o0.frags_i;
+                        o.oob += o0.oob;
+                        o.px0 = min(o.px0, o0.px0);
+                        o.px1 = max(o.px1, o0.px1);
+                        o0 = RowOut{0, 0, 0xFFFFFFFFu, 0};
+                    }
+                    acc_fi += o.frags_i;
+                    acc_oob += o.oob;
+                    mark_band(band, o, J, word, bit);
+                }
+                // Band 0 not visited (no row y > 0): flush the row-0 walk of
+                // lane 0.  The test is made warp-uniform before the shuffles.
+                const bool pend0 =
+                    __shfl_sync(0xFFFFFFFFu, (o0.frags_i || o0.oob || o0.px0 < o0.px1) ? 1 : 0, 0) != 0;
+                if (pend0) {
+                    acc_fi += o0.frags_i;
+                    acc_oob += o0.oob;
+                    RowOut z{0, 0, __shfl_sync(0xFFFFFFFFu, o0.px0, 0), __shfl_sync(0xFFFFFFFFu, o0.px1, 0)};
+                    if (lane != 0) z = RowOut{0, 0, 0xFFFFFFFFu, 0};
+                    mark_band(0, z, J, word, bit);
                 }
             }
+        }
+        __syncwarp();
+        {
+            const uint4 *src = reinterpret_cast<const uint4 *>(R);
+            uint4 *dst = reinterpret_cast<uint4 *>(rprims + p);
+            if (lane < sizeof(RasterPrim) / 16) dst[lane] = src[lane];
         }
     }
     flush();
@@ -632,33 +872,49 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
     return cudaGetLastError();
 }
 
+size_t scan64_scratch_words(uint32_t n) {
+    return (n + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS) + 1;
+}
+
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, const uint32_t *nprims_dev, uint32_t *mask,
-                         StatsDev *stats, int nsm, cudaStream_t s) {
+                         PrimRec *prims, const uint32_t *nprims_dev, uint32_t *tri_words,
+                         unsigned long long *tri_wbase, unsigned long long *scan64,
+                         unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
+                         RasterPrim *rprims, uint32_t *mask, StatsDev *stats, uint32_t *counters,
+                         int nsm, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    uint32_t blocks = min((nt + 127) / 128, (uint32_t)nsm * 16);
-    k_setup<<<blocks, 128, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool, prims, stats);
+    uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
+    k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
+                                                prims, tri_words, stats);
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // Row-record offsets of the input triangles (64-bit: the total may not fit 32).
+    const uint32_t nb = (nt + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS);
+    k_scan64_blocks<<<nb, SCAN_THREADS, 0, s>>>(tri_words, tri_wbase, nt, scan64);
+    k_scan64_sums<<<1, 1024, 0, s>>>(scan64, nb, rows_total);
+    k_scan64_add<<<nb, SCAN_THREADS, 0, s>>>(tri_wbase, nt, scan64);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // one warp per output triangle; the count is only known on the device
     uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
-    k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, nprims_dev, tile_w, mask, stats);
+    k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, nprims_dev, tile_w, tri_wbase, rows, rows_cap,
+                                  rprims, mask, stats, counters);
     return cudaGetLastError();
 }
 
 cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,
-                          const DrawDev *draws, const PrimRec *prims, const uint32_t *tcnt,
-                          const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
-                          uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
-                          cudaStream_t s) {
+                          const DrawDev *draws, const PrimRec *prims, const RasterPrim *rprims,
+                          const uint32_t *rows, const uint32_t *tcnt, const uint32_t *toff,
+                          const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
+                          StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     switch (tile_w) {
-        case 8: return launch_raster_tw8(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        case 16: return launch_raster_tw16(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        case 64: return launch_raster_tw64(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        default: return launch_raster_tw32(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 8: return launch_raster_tw8(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 16: return launch_raster_tw16(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 64: return launch_raster_tw64(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        default: return launch_raster_tw32(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
     }
 }
 

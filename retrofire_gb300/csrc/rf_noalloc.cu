@@ -54,8 +54,17 @@ constexpr size_t OFF_POOL = al(OFF_SCAN + 64 * 4);
 constexpr size_t OFF_PRIMS =
     al(OFF_POOL + (size_t)RF_NOALLOC_MAX_TRIS * RF_POLY_STORE * sizeof(PolyVert));
 constexpr size_t OFF_MASK = al(OFF_PRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(PrimRec));
-constexpr size_t SCRATCH_END = al(OFF_MASK + (size_t)MAX_TILES * MASK_WORDS * 4);
-static_assert(SCRATCH_END <= RF_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds its stated size");
+constexpr size_t OFF_TRIW = al(OFF_MASK + (size_t)MAX_TILES * MASK_WORDS * 4);
+constexpr size_t OFF_TRIB = al(OFF_TRIW + (size_t)RF_NOALLOC_MAX_TRIS * 4);
+constexpr size_t OFF_SCAN64 = al(OFF_TRIB + (size_t)RF_NOALLOC_MAX_TRIS * 8);
+constexpr size_t OFF_ROWTOT = al(OFF_SCAN64 + 64 * 8);
+constexpr size_t OFF_RPRIMS = al(OFF_ROWTOT + 8);
+constexpr size_t OFF_ROWS =
+    al(OFF_RPRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(RasterPrim));
+// The rest of the area holds row records; triangles whose records do not
+// fit are rasterised from their setup records instead (same results).
+constexpr size_t ROWS_WORDS = (RF_NOALLOC_SCRATCH_BYTES - OFF_ROWS) / 4;
+static_assert(OFF_ROWS + (1u << 20) <= RF_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds its stated size");
 
 constexpr int MAX_DEVICES = 64;
 void *g_addr[MAX_DEVICES];
@@ -194,6 +203,12 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     PolyVert *pool = reinterpret_cast<PolyVert *>(base + OFF_POOL);
     PrimRec *prims = reinterpret_cast<PrimRec *>(base + OFF_PRIMS);
     uint32_t *mask = reinterpret_cast<uint32_t *>(base + OFF_MASK);
+    uint32_t *triw = reinterpret_cast<uint32_t *>(base + OFF_TRIW);
+    unsigned long long *trib = reinterpret_cast<unsigned long long *>(base + OFF_TRIB);
+    unsigned long long *scan64 = reinterpret_cast<unsigned long long *>(base + OFF_SCAN64);
+    unsigned long long *rowtot = reinterpret_cast<unsigned long long *>(base + OFF_ROWTOT);
+    RasterPrim *rprims = reinterpret_cast<RasterPrim *>(base + OFF_RPRIMS);
+    uint32_t *rows = reinterpret_cast<uint32_t *>(base + OFF_ROWS);
 
     // ---- zero what the kernels accumulate into, then the pass itself
     NA_CK(cudaMemsetAsync(sd, 0, sizeof(StatsDev), s));
@@ -211,10 +226,12 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
                                cnt, nsm, s));
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
-                                cnt + RF_CNT_PRIMS, mask, sd, nsm, s));
+                                cnt + RF_CNT_PRIMS, triw, trib, scan64, rowtot, rows, ROWS_WORDS,
+                                rprims, mask, sd, cnt, nsm, s));
         const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
                           flags->depth_write;
-        NA_CK(rfk::launch_raster(TILE_W, shader, fast, jd, 1, dd, prims, tcnt, toff, mask, ntiles,
+        NA_CK(rfk::launch_raster(TILE_W, shader, fast, jd, 1, dd, prims, rprims, rows, tcnt, toff,
+                                 mask, ntiles,
                                  cnt + RF_CNT_QUEUE, sd, WARPS, nsm, s));
     }
     if (stats) {

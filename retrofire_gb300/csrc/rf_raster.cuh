@@ -100,42 +100,15 @@ struct TileCtx {
     unsigned long long frags_o;
 };
 
-// The lane's scanline j of half H (raster.rs:84-113), clipped to the tile,
-// then its fragments (raster.rs:60-69) into the tile (target.rs:163-198).
-// FAST: the default context (depth test Less, colour and depth writes on).
+// Fragments a..b-1 of one scanline into the tile (raster.rs:60-69,
+// target.rs:163-198): v = varyings of fragment a, stepped by dv per pixel.
 template <int KIND, bool FAST>
-__device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec *__restrict__ H,
-                                     uint32_t j) {
+__device__ __forceinline__ void pixels(TileCtx &T, const DrawDev &d, float *v, const float *dv,
+                                       uint32_t a, uint32_t b) {
     constexpr int NC = Kind<KIND>::NC;
-    const float lx = row_value(H, RF_R_LX, j);
-    const float rx = row_value(H, RF_R_RX, j);
-    const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-    const uint64_t xs = as_usize(x0r);
-    uint64_t xe = as_usize(x1r);
-    if (xe < xs) xe = xs;
-    if (xs >= T.tx1) return;
-    uint64_t nfr = xe - xs;
-    const uint32_t cnt = as_u32(fsub(x1r, x0r));
-    if (cnt < nfr) nfr = cnt;
-    const uint64_t send = xs + nfr;  // xs < 2^32 here, no overflow
-    const uint32_t a = (uint32_t)(xs > T.tx0 ? xs : T.tx0);
-    const uint32_t b = (uint32_t)(send < (uint64_t)T.tx1 ? send : (uint64_t)T.tx1);
-    if (a >= b) return;
-    // v0 = left.next(); v0 = v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:88-102),
-    // then k0 pixel steps to the tile's first column.
-    const float tshift = fsub(x0r, lx);
-    const uint32_t k0 = a - (uint32_t)xs;
-    float v[NC], dv[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-        dv[c] = H->dvdx[c];
-        const float c0 = row_value(H, RF_R_C + c, j);
-        const float adj = fadd(c0, fmul(fsub(fadd(c0, dv[c]), c0), tshift));
-        v[c] = jump(adj, dv[c], k0);
-    }
     uint32_t idx = (a - T.tx0) * RF_TILE_H + T.lane;
     const uint32_t end = (b - T.tx0) * RF_TILE_H + T.lane;
-    if (FAST) {
+    if constexpr (FAST) {
         // Two pixels per iteration: their depth tests and shading are
         // independent; only the running sums chain from pixel to pixel.
         uint32_t nout = 0;
@@ -167,30 +140,69 @@ __device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec
             }
         }
         T.frags_o += nout;
-        return;
+    } else {
+        for (; idx != end; idx += RF_TILE_H) {
+            const float z = v[0];
+            bool pass = true;
+            if (T.has_depth) {
+                const float cur = T.sdep[idx];
+                switch (T.depth_test) {  // ctx.rs:86-89
+                    case RF_K_DEPTH_NONE: pass = true; break;
+                    case RF_K_DEPTH_LESS: pass = cur < z; break;
+                    case RF_K_DEPTH_EQUAL: pass = cur == z; break;
+                    default: pass = cur > z; break;
+                }
+            }
+            if (pass) {
+                if (T.color_write) {
+                    T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                    T.frags_o += 1;
+                }
+                if (T.has_depth && T.depth_write) T.sdep[idx] = z;
+            }
+    #pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
+        }
     }
-    for (; idx != end; idx += RF_TILE_H) {
-        const float z = v[0];
-        bool pass = true;
-        if (T.has_depth) {
-            const float cur = T.sdep[idx];
-            switch (T.depth_test) {  // ctx.rs:86-89
-                case RF_K_DEPTH_NONE: pass = true; break;
-                case RF_K_DEPTH_LESS: pass = cur < z; break;
-                case RF_K_DEPTH_EQUAL: pass = cur == z; break;
-                default: pass = cur > z; break;
-            }
-        }
-        if (pass) {
-            if (T.color_write) {
-                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
-                T.frags_o += 1;
-            }
-            if (T.has_depth && T.depth_write) T.sdep[idx] = z;
-        }
+}
+
+// The lane's scanline j of half H (raster.rs:84-113), clipped to the tile,
+// then its fragments (raster.rs:60-69) into the tile (target.rs:163-198).
+// FAST: the default context (depth test Less, colour and depth writes on).
+template <int KIND, bool FAST>
+__device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec *__restrict__ H,
+                                     uint32_t j) {
+    constexpr int NC = Kind<KIND>::NC;
+    const float lx = row_value(H, RF_R_LX, j);
+    const float rx = row_value(H, RF_R_RX, j);
+    const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
+    // xs..xe as `as usize` (target.rs:259-262), zip-truncated to the
+    // fragment count, clipped to the tile.  32-bit saturating casts give the
+    // same clipped range as 64-bit ones (tile columns are < 2^16), and keep
+    // the conversions off the FP64 pipe.
+    const uint32_t xs = as_u32(x0r);
+    if (xs >= T.tx1) return;
+    uint32_t xe = as_u32(x1r);
+    if (xe < xs) xe = xs;
+    uint32_t nfr = xe - xs;
+    const uint32_t cnt = as_u32(fsub(x1r, x0r));
+    if (cnt < nfr) nfr = cnt;
+    const uint32_t a = xs > T.tx0 ? xs : T.tx0;
+    const uint32_t b = nfr >= T.tx1 - xs ? T.tx1 : xs + nfr;
+    if (a >= b) return;
+    // v0 = left.next(); v0 = v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:88-102),
+    // then k0 pixel steps to the tile's first column.
+    const float tshift = fsub(x0r, lx);
+    const uint32_t k0 = a - xs;
+    float v[NC], dv[NC];
 #pragma unroll
-        for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
+    for (int c = 0; c < NC; ++c) {
+        dv[c] = H->dvdx[c];
+        const float c0 = row_value(H, RF_R_C + c, j);
+        const float adj = fadd(c0, fmul(fsub(fadd(c0, dv[c]), c0), tshift));
+        v[c] = jump(adj, dv[c], k0);
     }
+    pixels<KIND, FAST>(T, d, v, dv, a, b);
 }
 
 // Which scanline of a half lands on row y: row(j) = (y0r + j) as usize =
@@ -242,46 +254,121 @@ __device__ __forceinline__ void raster_prim_k(TileCtx &T, const DrawDev &d, cons
     }
 }
 
+// A triangle with row records: the lane's row record, loaded into
+// registers one triangle ahead of its use (the loads overlap the previous
+// triangle's pixels).
+template <int NC>
+struct RowPreT {
+    uint32_t w0;  // first pixel | end << 16; 0 when the row has no record
+    uint32_t hh;  // half of the scanline
+    float v[NC];
+};
+// Components held for a kernel: its kind's, or all for RF_K_ANY.
+template <int KIND>
+struct PreNC {
+    static constexpr int NC = KIND == RF_K_ANY ? RF_NC : Kind<KIND == RF_K_ANY ? 0 : KIND>::NC;
+};
+template <int KIND>
+using RowPre = RowPreT<PreNC<KIND>::NC>;
+
+template <int KIND>
+__device__ __forceinline__ RowPre<KIND> row_prefetch(const TileCtx &T, const RasterPrim *__restrict__ R,
+                                                     const uint32_t *__restrict__ rows) {
+    RowPre<KIND> q;
+    q.w0 = 0;
+    q.hh = 0;
+    if (!T.row_ok || (R->flags & (RF_RP_LIVE | RF_RP_ROWS)) != (RF_RP_LIVE | RF_RP_ROWS)) return q;
+    const uint32_t y = T.y;
+    uint32_t j;
+    if (y - R->y0 < R->c0) {
+        j = y - R->y0;
+    } else if (y - R->y1 < R->c1) {
+        j = R->c0 + (y - R->y1);
+        q.hh = 1;
+    } else {
+        return q;
+    }
+    const uint32_t *rec = rows + R->base + (size_t)j * R->stride;
+    q.w0 = __ldg(rec);
+    if (KIND != RF_K_ANY) {
+#pragma unroll
+        for (int c = 0; c < PreNC<KIND>::NC; ++c) q.v[c] = u2f(__ldg(rec + 1 + c));
+    } else {
+        const uint32_t nc = R->stride - 1;
+#pragma unroll
+        for (int c = 0; c < PreNC<KIND>::NC; ++c) q.v[c] = (uint32_t)c < nc ? u2f(__ldg(rec + 1 + c)) : 0.0f;
+    }
+    return q;
+}
+
+template <int KIND, bool FAST, int QN>
+__device__ __forceinline__ void raster_rows(TileCtx &T, const DrawDev &d, const RasterPrim *__restrict__ R,
+                                            const RowPreT<QN> &q) {
+    static_assert(QN >= Kind<KIND>::NC, "prefetched record too short");
+    constexpr int NC = Kind<KIND>::NC;
+    const uint32_t xs = q.w0 & 0xFFFFu, xe = q.w0 >> 16;
+    const uint32_t a = xs > T.tx0 ? xs : T.tx0;
+    const uint32_t b = xe < T.tx1 ? xe : T.tx1;
+    if (a >= b) return;
+    const uint32_t k0 = a - xs;
+    float v[NC], dv[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        dv[c] = R->dvdx[q.hh][c];
+        v[c] = jump(q.v[c], dv[c], k0);
+    }
+    pixels<KIND, FAST>(T, d, v, dv, a, b);
+}
+
+template <int KIND, bool FAST, int QN>
+__device__ __forceinline__ void raster_one(TileCtx &T, const DrawDev &d, const RasterPrim *__restrict__ R,
+                                           const PrimRec *__restrict__ P, const RowPreT<QN> &q) {
+    if (R->flags & RF_RP_ROWS) raster_rows<KIND, FAST, QN>(T, d, R, q);
+    else raster_prim_k<KIND, FAST>(T, d, P);
+}
+
 // KIND: the shader kind of every draw of the job, or RF_K_ANY (dispatch per
 // triangle).
 template <int KIND, bool FAST>
 __device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restrict__ draws,
-                                            const PrimRec *__restrict__ P) {
-    if (!P->live) return;
-    const DrawDev &d = draws[P->draw];
-    if (KIND != RF_K_ANY) {
-        raster_prim_k<KIND == RF_K_ANY ? 0 : KIND, FAST>(T, d, P);
-        return;
+                                            const RasterPrim *__restrict__ R,
+                                            const PrimRec *__restrict__ P, const RowPre<KIND> &q) {
+    if (!(R->flags & RF_RP_LIVE)) return;
+    const DrawDev &d = draws[R->draw];
+    if constexpr (KIND != RF_K_ANY) {
+        raster_one<KIND == RF_K_ANY ? 0 : KIND, FAST, PreNC<KIND>::NC>(T, d, R, P, q);
+    } else {
+    switch (R->kind) {
+        case RF_K_FLAT: raster_one<RF_K_FLAT, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
+        case RF_K_GOURAUD: raster_one<RF_K_GOURAUD, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
+        case RF_K_TEXTURED: raster_one<RF_K_TEXTURED, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
+        case RF_K_TEX_GOURAUD: raster_one<RF_K_TEX_GOURAUD, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
+        default: raster_one<RF_K_GOURAUD_SRGB, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
     }
-    switch (P->kind) {
-        case RF_K_FLAT: raster_prim_k<RF_K_FLAT, FAST>(T, d, P); break;
-        case RF_K_GOURAUD: raster_prim_k<RF_K_GOURAUD, FAST>(T, d, P); break;
-        case RF_K_TEXTURED: raster_prim_k<RF_K_TEXTURED, FAST>(T, d, P); break;
-        case RF_K_TEX_GOURAUD: raster_prim_k<RF_K_TEX_GOURAUD, FAST>(T, d, P); break;
-        default: raster_prim_k<RF_K_GOURAUD_SRGB, FAST>(T, d, P); break;
     }
 }
 
 // Walks a tile's bitmask in submission order: set bits of the mask words
-// (input triangles), each expanded to its clipped output triangles.
-// Warp-uniform state; every lane calls next() together.
+// (input triangles), each expanded to its clipped output triangles.  The
+// offsets of the next input triangle are loaded one triangle ahead, so
+// their latency overlaps the current triangle.  Warp-uniform state; every
+// lane calls next() together.
 struct PrimIter {
     const uint32_t *tmask;
     const uint32_t *toff;
     const uint32_t *tcnt;
     uint32_t nwords, tri_base, lane;
     uint32_t wb, word, bal, src, wv, p, pend;
-    bool started;
-    __device__ __forceinline__ uint32_t next() {
+    uint32_t la_off, la_cnt;  // loads in flight for the look-ahead triangle
+    bool started, has_la;
+    // Next set bit (input triangle, global index) or false.
+    __device__ __forceinline__ bool next_bit(uint32_t &gt) {
         for (;;) {
-            if (p < pend) return p++;
             if (wv) {
                 const uint32_t b = __ffs(wv) - 1;
                 wv &= wv - 1;
-                const uint32_t gt = tri_base + (wb + src) * 32 + b;
-                p = toff[gt];
-                pend = p + tcnt[gt];
-                continue;
+                gt = tri_base + (wb + src) * 32 + b;
+                return true;
             }
             if (bal) {
                 src = __ffs(bal) - 1;
@@ -291,19 +378,41 @@ struct PrimIter {
             }
             if (started) wb += 32;
             started = true;
-            if (wb >= nwords) return 0xFFFFFFFFu;
+            if (wb >= nwords) return false;
             word = wb + lane < nwords ? tmask[wb + lane] : 0u;
             bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
         }
     }
+    __device__ __forceinline__ void look_ahead() {
+        uint32_t gt;
+        has_la = next_bit(gt);
+        if (has_la) {
+            la_off = __ldg(toff + gt);
+            la_cnt = __ldg(tcnt + gt);
+        }
+    }
+    __device__ __forceinline__ void init() {
+        wb = word = bal = src = wv = p = pend = 0;
+        started = false;
+        look_ahead();
+    }
+    __device__ __forceinline__ uint32_t next() {
+        while (p >= pend) {
+            if (!has_la) return 0xFFFFFFFFu;
+            p = la_off;
+            pend = la_off + la_cnt;
+            look_ahead();
+        }
+        return p++;
+    }
 };
 
-// Asynchronous copy of one triangle record into this warp's staging slot
+// Asynchronous copy of one triangle header into this warp's staging slot
 // (16 bytes per lane; one commit group per call on every lane).
-__device__ __forceinline__ void stage_prim(PrimRec *slot, const PrimRec *src, uint32_t lane) {
-    static_assert(sizeof(PrimRec) % 16 == 0, "PrimRec must be a whole number of 16-byte chunks");
-    static_assert(sizeof(PrimRec) <= 64 * 16, "PrimRec is staged in at most two rounds");
-    constexpr uint32_t CHUNKS = sizeof(PrimRec) / 16;
+__device__ __forceinline__ void stage_prim(RasterPrim *slot, const RasterPrim *src, uint32_t lane) {
+    static_assert(sizeof(RasterPrim) % 16 == 0, "RasterPrim must be a whole number of 16-byte chunks");
+    static_assert(sizeof(RasterPrim) <= 64 * 16, "RasterPrim is staged in at most two rounds");
+    constexpr uint32_t CHUNKS = sizeof(RasterPrim) / 16;
     if (src) {
 #pragma unroll
         for (uint32_t c = lane; c < CHUNKS; c += 32) {
@@ -316,8 +425,9 @@ __device__ __forceinline__ void stage_prim(PrimRec *slot, const PrimRec *src, ui
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
-__device__ __forceinline__ void wait_staged_but_one() {
-    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+template <int N>
+__device__ __forceinline__ void wait_staged_but() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
     __syncwarp();
 }
 
@@ -327,18 +437,19 @@ __device__ __forceinline__ void wait_staged_but_one() {
 // default context (depth test Less, colour and depth writes) on a target
 // with depth.
 template <int TW, int KIND, bool FAST>
-__global__ void __launch_bounds__(RF_RASTER_MAX_THREADS)
+__global__ void __launch_bounds__(RF_RASTER_MAX_THREADS, 2)
 k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict__ draws,
-         const PrimRec *__restrict__ prims, const uint32_t *__restrict__ tcnt,
+         const PrimRec *__restrict__ prims, const RasterPrim *__restrict__ rprims,
+         const uint32_t *__restrict__ rows, const uint32_t *__restrict__ tcnt,
          const uint32_t *__restrict__ toff, const uint32_t *__restrict__ mask,
          uint32_t ntiles_total, uint32_t *__restrict__ tile_queue, StatsDev *__restrict__ stats) {
     using namespace rfr;
     extern __shared__ __align__(16) uint32_t smem[];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr uint32_t WARP_WORDS = 2 * TW * RF_TILE_H + 2 * (sizeof(PrimRec) / 4);
+    constexpr uint32_t WARP_WORDS = 2 * TW * RF_TILE_H + 3 * (sizeof(RasterPrim) / 4);
     uint32_t *scol = smem + warp * WARP_WORDS;
     float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
-    PrimRec *stage = reinterpret_cast<PrimRec *>(scol + 2 * TW * RF_TILE_H);
+    RasterPrim *stage = reinterpret_cast<RasterPrim *>(scol + 2 * TW * RF_TILE_H);
     for (;;) {
         uint32_t tile = 0;
         if (lane == 0) tile = atomicAdd(tile_queue, 1u);
@@ -403,27 +514,44 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         it.nwords = J.mask_words;
         it.tri_base = J.tri_base;
         it.lane = lane;
-        it.wb = it.word = it.bal = it.src = it.wv = it.p = it.pend = 0;
-        it.started = false;
+        it.init();
         // Double-buffered: the record of the next triangle is in flight
         // while the current one is rasterised.
-        uint32_t cur = it.next();
-        if (cur != 0xFFFFFFFFu) {
+        // Three staging slots: triangle i is rasterised while the header of
+        // i+2 is in flight and the row records of i+1 load into registers.
+        // Prims p0 (current), p1, p2 in slots s0, s1, s2; the slots rotate.
+        constexpr uint32_t NONE = 0xFFFFFFFFu;
+        uint32_t p0 = it.next();
+        if (p0 != NONE) {
             load_tile();
             loaded = true;
-            stage_prim(stage + 0, prims + cur, lane);
-            uint32_t nxt = it.next();
-            stage_prim(stage + 1, nxt != 0xFFFFFFFFu ? prims + nxt : nullptr, lane);
-            uint32_t slot = 0;
+            stage_prim(stage + 0, rprims + p0, lane);
+            uint32_t p1 = it.next();
+            stage_prim(stage + 1, p1 != NONE ? rprims + p1 : nullptr, lane);
+            uint32_t p2 = p1 != NONE ? it.next() : NONE;
+            stage_prim(stage + 2, p2 != NONE ? rprims + p2 : nullptr, lane);
+            wait_staged_but<2>();
+            RowPre<KIND> q = row_prefetch<KIND>(T, stage + 0, rows);
+            uint32_t s0 = 0, s1 = 1, s2 = 2;
             for (;;) {
-                wait_staged_but_one();
-                raster_prim<KIND, FAST>(T, draws, stage + slot);
+                wait_staged_but<1>();
+                RowPre<KIND> qn;
+                qn.w0 = 0;
+                qn.hh = 0;
+                if (p1 != NONE) qn = row_prefetch<KIND>(T, stage + s1, rows);
+                raster_prim<KIND, FAST>(T, draws, stage + s0, prims + p0, q);
                 __syncwarp();
-                if (nxt == 0xFFFFFFFFu) break;
-                const uint32_t after = it.next();
-                stage_prim(stage + slot, after != 0xFFFFFFFFu ? prims + after : nullptr, lane);
-                slot ^= 1u;
-                nxt = after;
+                if (p1 == NONE) break;
+                const uint32_t p3 = p2 != NONE ? it.next() : NONE;
+                stage_prim(stage + s0, p3 != NONE ? rprims + p3 : nullptr, lane);
+                q = qn;
+                p0 = p1;
+                p1 = p2;
+                p2 = p3;
+                const uint32_t t = s0;
+                s0 = s1;
+                s1 = s2;
+                s2 = t;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
         }
@@ -460,11 +588,12 @@ namespace rfk {
 
 template <int TW, int KIND, bool FAST>
 static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDev *draws,
-                                   const PrimRec *prims, const uint32_t *tcnt,
+                                   const PrimRec *prims, const RasterPrim *rprims,
+                                   const uint32_t *rows, const uint32_t *tcnt,
                                    const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
                                    uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
                                    cudaStream_t s) {
-    const size_t smem = (size_t)warps * (2 * TW * RF_TILE_H * 4 + 2 * sizeof(PrimRec));
+    const size_t smem = (size_t)warps * (2 * TW * RF_TILE_H * 4 + 3 * sizeof(RasterPrim));
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_raster<TW, KIND, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -477,8 +606,8 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
     const uint32_t need = (ntiles + warps - 1) / warps;
     if (blocks > need) blocks = need;
     if (blocks == 0) blocks = 1;
-    k_raster<TW, KIND, FAST><<<blocks, warps * 32, smem, s>>>(jobs, nj, draws, prims, tcnt, toff, mask,
-                                                       ntiles, queue, stats);
+    k_raster<TW, KIND, FAST><<<blocks, warps * 32, smem, s>>>(jobs, nj, draws, prims, rprims, rows,
+                                                             tcnt, toff, mask, ntiles, queue, stats);
     return cudaGetLastError();
 }
 
@@ -488,24 +617,25 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
 template <int TW>
 static cudaError_t launch_raster_for_width(int kind, bool fast, const JobDev *jobs, uint32_t nj,
                                            const DrawDev *draws, const PrimRec *prims,
+                                           const RasterPrim *rprims, const uint32_t *rows,
                                            const uint32_t *tcnt, const uint32_t *toff,
                                            const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
                                            StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
     if (!fast)
-        return launch_raster_k<TW, RF_K_ANY, false>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        return launch_raster_k<TW, RF_K_ANY, false>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
     switch (kind) {
         case RF_K_FLAT:
-            return launch_raster_k<TW, RF_K_FLAT, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_FLAT, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
         case RF_K_GOURAUD:
-            return launch_raster_k<TW, RF_K_GOURAUD, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_GOURAUD, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
         case RF_K_TEXTURED:
-            return launch_raster_k<TW, RF_K_TEXTURED, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_TEXTURED, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
         case RF_K_TEX_GOURAUD:
-            return launch_raster_k<TW, RF_K_TEX_GOURAUD, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_TEX_GOURAUD, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
         case RF_K_GOURAUD_SRGB:
-            return launch_raster_k<TW, RF_K_GOURAUD_SRGB, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_GOURAUD_SRGB, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
         default:
-            return launch_raster_k<TW, RF_K_ANY, true>(jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_ANY, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
     }
 }
 

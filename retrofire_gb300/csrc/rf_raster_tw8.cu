@@ -3,10 +3,12 @@
 
 namespace rfk {
 cudaError_t launch_raster_tw8(int kind, bool fast, const JobDev *jobs, uint32_t nj, const DrawDev *draws,
-                              const PrimRec *prims, const uint32_t *tcnt, const uint32_t *toff,
+                              const PrimRec *prims, const RasterPrim *rprims, const uint32_t *rows,
+                              const uint32_t *tcnt, const uint32_t *toff,
                               const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
                               StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
-    return launch_raster_for_width<8>(kind, fast, jobs, nj, draws, prims, tcnt, toff, mask, ntiles, queue,
+    return launch_raster_for_width<8>(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask,
+                                       ntiles, queue,
                                        stats, warps, nsm, s);
 }
 }  // namespace rfk
