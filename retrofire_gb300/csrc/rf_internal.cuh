@@ -100,10 +100,12 @@ struct PrimRec {
 
 // Row records: for every scanline of a triangle that lands on a row of the
 // target, word 0 = first pixel | (one past the last pixel) << 16 (the span
-// xs..xe after zip truncation and clipping to the target; 0 when empty) and
+// xs..xe after zip truncation and clipping to the target; 0 when empty),
 // words 1..NC = the varyings of the span's first fragment after the x0
-// adjustment of raster.rs:102.  Written once by the binning pass from a
-// sequential walk of the scanlines (the reference's own running sums).
+// adjustment of raster.rs:102, and words NC+1..2NC = the varyings at the
+// span's first tile boundary (the first pixel of the next tile column).
+// Written once by the binning pass from a sequential walk of the scanlines
+// (the reference's own running sums).
 //
 // RasterPrim: the rasteriser's view of one output triangle.
 #define RF_RP_LIVE 1u
@@ -113,7 +115,7 @@ struct RasterPrim {
     uint32_t flags;
     int32_t kind;
     uint32_t base;    // word offset of the first row record
-    uint32_t stride;  // words per row record (1 + NC)
+    uint32_t stride;  // words per row record (1 + 2 NC)
     uint32_t y0, c0;  // upper half: rows y0 .. y0+c0-1, records 0 .. c0-1
     uint32_t y1, c1;  // lower half: rows y1 .. y1+c1-1, records c0 .. c0+c1-1
     float dvdx[2][RF_NC];

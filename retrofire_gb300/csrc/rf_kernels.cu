@@ -546,7 +546,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     const int64_t in = min((int64_t)H.n, max((int64_t)0, (int64_t)J.h - Y));
                     rows += (uint32_t)in;
                 }
-                const uint64_t w = regular ? (uint64_t)rows * (1u + nc) : 0u;
+                const uint64_t w = regular ? (uint64_t)rows * (1u + 2u * nc) : 0u;
                 if (w < 0x40000000ull && (uint64_t)words + w < 0x40000000ull) {
                     P.rwords = (uint32_t)w;
                     words += (uint32_t)w;
@@ -688,7 +688,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             const uint32_t word = tl >> 5, bit = 1u << (tl & 31);
             const uint32_t nc = 1 + nattr_of(P->kind);
             const uint32_t nr = RF_R_C + nc;
-            const uint32_t stride = 1 + nc;
+            const uint32_t stride = 1 + 2 * nc;
             bool regular = P->rwords != 0;
             unsigned long long base = 0;
             if (regular) {
@@ -763,11 +763,19 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                             }
                             uint32_t *rec = rows + base + (size_t)(rec_off + (uint32_t)(y - Y)) * stride;
                             rec[0] = w0;
-                            // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102)
+                            // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102),
+                            // and the varyings at the span's first tile boundary.
                             const float tshift = fsub(x0r, lx);
+                            const uint32_t kb = w0 ? (o.px0 / tile_w + 1) * tile_w - o.px0 : 0u;
+                            const bool crosses = w0 && o.px0 + kb < o.px1;
+                            const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
                             for (uint32_t c = 0; c < nc; ++c) {
                                 const float cv = T[i][RF_R_C + c], dv = H->dvdx[c];
-                                rec[1 + c] = f2u(fadd(cv, fmul(fsub(fadd(cv, dv), cv), tshift)));
+                                const float v0 = fadd(cv, fmul(fsub(fadd(cv, dv), cv), tshift));
+                                rec[1 + c] = f2u(v0);
+                                float vb = v0;
+                                for (uint32_t k = 0; k < ksteps; ++k) vb = fadd(vb, dv);  // Iter::next
+                                rec[1 + nc + c] = f2u(vb);
                             }
                         }
                         acc_fi += o.frags_i;

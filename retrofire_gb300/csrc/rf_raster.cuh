@@ -92,6 +92,7 @@ struct TileCtx {
     uint32_t y;       // this lane's row
     uint32_t tx0;     // first column of the tile
     uint32_t tx1;     // one past the last column of the tile inside the target
+    uint32_t tw;      // tile width (a power of two)
     bool row_ok;
     bool has_depth;
     int32_t depth_test;
@@ -109,35 +110,52 @@ __device__ __forceinline__ void pixels(TileCtx &T, const DrawDev &d, float *v, c
     uint32_t idx = (a - T.tx0) * RF_TILE_H + T.lane;
     const uint32_t end = (b - T.tx0) * RF_TILE_H + T.lane;
     if constexpr (FAST) {
-        // Two pixels per iteration: their depth tests and shading are
-        // independent; only the running sums chain from pixel to pixel.
+        // Four pixels per iteration: their depths are loaded together (this
+        // lane alone writes its row, so they cannot change meanwhile); only
+        // the running sums chain from pixel to pixel.
         uint32_t nout = 0;
-        for (; idx + RF_TILE_H < end; idx += 2 * RF_TILE_H) {
-            float v1[NC];
-#pragma unroll
-            for (int c = 0; c < NC; ++c) v1[c] = fadd(v[c], dv[c]);
+        for (; idx + 3 * RF_TILE_H < end; idx += 4 * RF_TILE_H) {
             const float c0 = T.sdep[idx], c1 = T.sdep[idx + RF_TILE_H];
-            const float z0 = v[0], z1 = v1[0];
-            if (c0 < z0) {  // ctx.rs:86-89 with Some(Less)
+            const float c2 = T.sdep[idx + 2 * RF_TILE_H], c3 = T.sdep[idx + 3 * RF_TILE_H];
+            float v1[NC], v2[NC], v3[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                v1[c] = fadd(v[c], dv[c]);
+                v2[c] = fadd(v1[c], dv[c]);
+                v3[c] = fadd(v2[c], dv[c]);
+            }
+            if (c0 < v[0]) {  // ctx.rs:86-89 with Some(Less)
                 T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
-                T.sdep[idx] = z0;
+                T.sdep[idx] = v[0];
                 ++nout;
             }
-            if (c1 < z1) {
+            if (c1 < v1[0]) {
                 T.scol[idx + RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
-                T.sdep[idx + RF_TILE_H] = z1;
+                T.sdep[idx + RF_TILE_H] = v1[0];
+                ++nout;
+            }
+            if (c2 < v2[0]) {
+                T.scol[idx + 2 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v2), T.fmt);
+                T.sdep[idx + 2 * RF_TILE_H] = v2[0];
+                ++nout;
+            }
+            if (c3 < v3[0]) {
+                T.scol[idx + 3 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v3), T.fmt);
+                T.sdep[idx + 3 * RF_TILE_H] = v3[0];
                 ++nout;
             }
 #pragma unroll
-            for (int c = 0; c < NC; ++c) v[c] = fadd(v1[c], dv[c]);
+            for (int c = 0; c < NC; ++c) v[c] = fadd(v3[c], dv[c]);
         }
-        if (idx != end) {
+        for (; idx != end; idx += RF_TILE_H) {
             const float z = v[0];
             if (T.sdep[idx] < z) {
                 T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
                 T.sdep[idx] = z;
                 ++nout;
             }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
         }
         T.frags_o += nout;
     } else {
@@ -261,7 +279,8 @@ template <int NC>
 struct RowPreT {
     uint32_t w0;  // first pixel | end << 16; 0 when the row has no record
     uint32_t hh;  // half of the scanline
-    float v[NC];
+    float v[NC];  // varyings at the span's first pixel
+    float vb[NC]; // ... and at its first tile boundary
 };
 // Components held for a kernel: its kind's, or all for RF_K_ANY.
 template <int KIND>
@@ -291,12 +310,19 @@ __device__ __forceinline__ RowPre<KIND> row_prefetch(const TileCtx &T, const Ras
     const uint32_t *rec = rows + R->base + (size_t)j * R->stride;
     q.w0 = __ldg(rec);
     if (KIND != RF_K_ANY) {
+        constexpr int NC = PreNC<KIND>::NC;
 #pragma unroll
-        for (int c = 0; c < PreNC<KIND>::NC; ++c) q.v[c] = u2f(__ldg(rec + 1 + c));
+        for (int c = 0; c < NC; ++c) {
+            q.v[c] = u2f(__ldg(rec + 1 + c));
+            q.vb[c] = u2f(__ldg(rec + 1 + NC + c));
+        }
     } else {
-        const uint32_t nc = R->stride - 1;
+        const uint32_t nc = (R->stride - 1) / 2;
 #pragma unroll
-        for (int c = 0; c < PreNC<KIND>::NC; ++c) q.v[c] = (uint32_t)c < nc ? u2f(__ldg(rec + 1 + c)) : 0.0f;
+        for (int c = 0; c < PreNC<KIND>::NC; ++c) {
+            q.v[c] = (uint32_t)c < nc ? u2f(__ldg(rec + 1 + c)) : 0.0f;
+            q.vb[c] = (uint32_t)c < nc ? u2f(__ldg(rec + 1 + nc + c)) : 0.0f;
+        }
     }
     return q;
 }
@@ -310,12 +336,15 @@ __device__ __forceinline__ void raster_rows(TileCtx &T, const DrawDev &d, const 
     const uint32_t a = xs > T.tx0 ? xs : T.tx0;
     const uint32_t b = xe < T.tx1 ? xe : T.tx1;
     if (a >= b) return;
-    const uint32_t k0 = a - xs;
+    // The span starts in this tile (k = 0 from its first pixel) or enters it
+    // at a tile boundary at or after its first one (k steps from there).
+    const bool first = a == xs;
+    const uint32_t k = first ? 0u : a - ((xs & ~(T.tw - 1u)) + T.tw);
     float v[NC], dv[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         dv[c] = R->dvdx[q.hh][c];
-        v[c] = jump(q.v[c], dv[c], k0);
+        v[c] = jump(first ? q.v[c] : q.vb[c], dv[c], k);
     }
     pixels<KIND, FAST>(T, d, v, dv, a, b);
 }
@@ -465,6 +494,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         T.lane = lane;
         T.tx0 = txi * TW;
         T.tx1 = min(T.tx0 + (uint32_t)TW, J.w);
+        T.tw = TW;
         T.y = tyi * RF_TILE_H + lane;
         T.row_ok = T.y < J.h;
         T.has_depth = J.depth != nullptr;
