@@ -285,6 +285,7 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    k0 = dev.counts()["kernels"]
     clocks.start()
     with torch.cuda.stream(stream):
         for i in range(args.steps):
@@ -295,6 +296,7 @@ def run_gpu(args):
             evs[i][1].record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    launches = dev.counts()["kernels"] - k0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     stage, nfr = dev.stage_ms()
     dev.set_timing(False)
@@ -331,7 +333,7 @@ def run_gpu(args):
                          "alg_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 7 * args.steps,
+            "gpu_launches": launches,
             "clocks": clk,
         }
         print(json.dumps(line))

@@ -174,6 +174,47 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
                           const float viewport[16], rf_target target,
                           const rf_context_flags *flags, rf_stats *stats);
 
+/* ---- batched scenes ----------------------------------------------------
+ * A scene = one target and the render() calls that draw into it, in order
+ * (a frame of demos/src/bin/crates.rs:114-133).  rf_render_batch renders
+ * njobs scenes as one pass of the pipeline: every stage runs once over the
+ * triangles of all scenes and one persistent raster launch takes the tiles
+ * of every target from a single queue.  The result for each scene equals
+ * rf_render_draws on it alone.  A target may appear in at most one job of a
+ * batch (RF_ERR_BAD_ARG otherwise).  stats: NULL queues the work (stats
+ * accumulate for rf_ctx_take_stats), else njobs entries, one per scene,
+ * stored after the batch completes. */
+typedef struct {
+    rf_target target;
+    uint32_t ndraws;
+    const rf_draw *draws;
+    float viewport[16];       /* Mat4<Ndc, Screen> of the scene */
+    rf_context_flags flags;
+} rf_job;
+rf_status rf_render_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, rf_stats *stats);
+
+/* CUDA-graph replay.  When enabled, the launch sequence of a frame is
+ * captured once per frame shape (draw, job, vertex, triangle and tile
+ * counts, tiling) and replayed with one graph launch when a frame of the
+ * same shape comes again; the per-frame data (matrices, targets, clears)
+ * are uploaded before the replay.  Stage timing (rf_ctx_set_timing) turns
+ * replay off. */
+rf_status rf_ctx_set_graphs(rf_ctx *ctx, int32_t enable);
+/* Counters of the context so far: GPU kernels launched by the library
+ * (directly or as graph nodes), graph launches, graphs cached.  NULL
+ * pointers are skipped. */
+rf_status rf_ctx_counts(rf_ctx *ctx, uint64_t *kernels, uint64_t *graph_launches,
+                        uint32_t *graphs_cached);
+
+/* Tiling autotuner: renders the batch with every tile width (8, 16, 32, 64)
+ * and rasteriser warps per block (4, 8), reps timed runs each after a
+ * warm-up, keeps the fastest on the context and returns it.  Every target
+ * is snapshotted first and restored after each trial and at the end, and
+ * the trials' stats are not reported, so the call leaves no trace but the
+ * tiling. */
+rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint32_t reps,
+                          uint32_t *tile_w, uint32_t *warps, float *best_ms);
+
 /* ---- rendering without device allocation ------------------------------
  * No counterpart in the reference: retrofire allocates freely on the CPU.
  * For callers that must not call cudaMalloc while rendering — a frame loop

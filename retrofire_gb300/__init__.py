@@ -68,6 +68,11 @@ class Draw(C.Structure):
                 ("uniforms", Uniforms)]
 
 
+class Job(C.Structure):
+    _fields_ = [("target", C.c_uint64), ("ndraws", C.c_uint32), ("draws", C.POINTER(Draw)),
+                ("viewport", C.c_float * 16), ("flags", Flags)]
+
+
 # Exported symbols of include/rfgpu.h with their ctypes signatures.
 _P = C.c_void_p
 _SIGS = {
@@ -95,6 +100,11 @@ _SIGS = {
                   C.c_uint64, C.POINTER(Flags), C.POINTER(CStats)],
     "rf_render_draws": [_P, C.POINTER(Draw), C.c_uint32, C.POINTER(C.c_float), C.c_uint64,
                         C.POINTER(Flags), C.POINTER(CStats)],
+    "rf_render_batch": [_P, C.POINTER(Job), C.c_uint32, C.POINTER(CStats)],
+    "rf_ctx_set_graphs": [_P, C.c_int32],
+    "rf_ctx_counts": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)],
+    "rf_ctx_autotune": [_P, C.POINTER(Job), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
+                        C.POINTER(C.c_uint32), C.POINTER(C.c_float)],
     # device pointers throughout; see include/rfgpu.h
     "rf_render_noalloc": [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.c_uint32, C.c_int32,
                           C.POINTER(C.c_float), C.c_uint32, _P, C.c_uint32, C.c_uint32,
@@ -217,6 +227,15 @@ class Device:
         fr = C.c_uint32()
         _check(lib().rf_ctx_stage_ms(self.ptr, out, C.byref(fr)), "rf_ctx_stage_ms")
         return dict(zip(STAGES, list(out))), fr.value
+
+    def set_graphs(self, enable=True):
+        _check(lib().rf_ctx_set_graphs(self.ptr, int(bool(enable))), "rf_ctx_set_graphs")
+
+    def counts(self):
+        """{kernels, graph_launches, graphs_cached} of this context so far."""
+        k, n, c = C.c_uint64(), C.c_uint64(), C.c_uint32()
+        _check(lib().rf_ctx_counts(self.ptr, C.byref(k), C.byref(n), C.byref(c)), "rf_ctx_counts")
+        return {"kernels": k.value, "graph_launches": n.value, "graphs_cached": c.value}
 
     def take_stats(self):
         cs = CStats()
@@ -404,3 +423,65 @@ def render_draws(draws, to_screen, target, ctx=None, sync_stats=True):
     st = Stats.from_c(cs)
     ctx.stats += st
     return st
+
+
+class Scene:
+    """One job of a batch: a target, its Context flags and viewport, and the
+    render() calls into it, in order.  draws: list of (Mesh, Shader, mvp)."""
+
+    def __init__(self, target, draws, to_screen, ctx=None):
+        self.target, self.draws, self.ctx = target, list(draws), ctx or Context()
+        self.to_screen = np.ascontiguousarray(to_screen, np.float32).reshape(-1)
+
+
+def _jobs(scenes):
+    jobs = (Job * len(scenes))()
+    keep = []
+    for j, sc in zip(jobs, scenes):
+        arr = (Draw * max(1, len(sc.draws)))()
+        for i, (mesh, shader, mvp) in enumerate(sc.draws):
+            arr[i].mesh = mesh.handle
+            arr[i].shader = shader.kind
+            arr[i].uniforms = shader.uniforms(mvp)
+        keep.append(arr)
+        j.target = sc.target.handle
+        j.ndraws = len(sc.draws)
+        j.draws = C.cast(arr, C.POINTER(Draw))
+        j.viewport[:] = [float(x) for x in sc.to_screen]
+        j.flags = sc.ctx.flags()
+    return jobs, keep
+
+
+def render_batch(scenes, device=None, sync_stats=True):
+    """rf_render_batch: every scene rendered as one pass over all targets.
+    Returns one Stats per scene (added into each scene's ctx.stats), or None
+    when sync_stats is false (the work is only queued)."""
+    if not scenes:
+        return []
+    dev = device or scenes[0].target.dev
+    jobs, keep = _jobs(scenes)
+    out = (CStats * len(scenes))() if sync_stats else None
+    _check(lib().rf_render_batch(dev.ptr, jobs, len(scenes),
+                                 C.cast(out, C.POINTER(CStats)) if out is not None else None),
+           "rf_render_batch")
+    del keep
+    if out is None:
+        return None
+    res = []
+    for sc, cs in zip(scenes, out):
+        st = Stats.from_c(cs)
+        sc.ctx.stats += st
+        res.append(st)
+    return res
+
+
+def autotune(scenes, reps=3, device=None):
+    """rf_ctx_autotune over a batch: returns (tile_w, warps, best_ms) and
+    keeps that tiling on the device context; the targets are unchanged."""
+    dev = device or scenes[0].target.dev
+    jobs, keep = _jobs(scenes)
+    tw, wp, ms = C.c_uint32(), C.c_uint32(), C.c_float()
+    _check(lib().rf_ctx_autotune(dev.ptr, jobs, len(scenes), reps, C.byref(tw), C.byref(wp),
+                                 C.byref(ms)), "rf_ctx_autotune")
+    del keep
+    return tw.value, wp.value, ms.value

@@ -45,6 +45,18 @@ struct DevBuf {
     size_t cap = 0;
 };
 
+// An instantiated launch sequence and the frame shape it was captured for.
+struct GraphKey {
+    uint64_t v[13];
+    bool operator==(const GraphKey &o) const { return memcmp(v, o.v, sizeof v) == 0; }
+};
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec;
+    uint64_t used;
+};
+constexpr size_t RF_GRAPH_CACHE = 8;
+
 }  // namespace
 
 struct rf_ctx {
@@ -58,7 +70,13 @@ struct rf_ctx {
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
-    DevBuf triw, trib, scan64, rowtot, rows, rprims;
+    DevBuf triw, trib, scan64, rowtot, rows, rprims, jstats;
+    // CUDA graphs of the launch sequence, keyed by frame shape (graph mode).
+    bool graphs = false;
+    uint64_t gen = 0;  // bumped whenever a scratch buffer moves
+    std::vector<GraphEntry> gcache;
+    uint64_t gclock = 0, graph_launches = 0;
+    uint64_t kernels = 0;  // kernels launched (directly or inside graphs)
     // Row-record capacity (words): grown when a frame asked for more, which
     // the library learns from an asynchronous read-back of the total.
     uint64_t rows_cap = 0;
@@ -93,12 +111,17 @@ rf_status cuda_fail(rf_ctx *c, cudaError_t e, const char *what) {
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
     } while (0)
 
+void graphs_drop(rf_ctx *ctx);
+
 rf_status ensure(rf_ctx *ctx, DevBuf &b, size_t bytes) {
     if (bytes <= b.cap && b.p) return RF_OK;
     size_t cap = b.cap ? b.cap : 4096;
     while (cap < bytes) cap *= 2;
+    // The old buffer may still be in use, and cached graphs point at it.
+    CK(cudaStreamSynchronize(ctx->stream));
+    graphs_drop(ctx);
+    ctx->gen += 1;
     if (b.p) {
-        CK(cudaStreamSynchronize(ctx->stream));  // the old buffer may still be in use
         CK(cudaFree(b.p));
         b.p = nullptr;
         b.cap = 0;
@@ -167,89 +190,159 @@ rf_status init_stats(rf_ctx *ctx) {
     return RF_OK;
 }
 
-// One frame: a single job (target) with ndraws draws, in order.
-rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const float vp[16],
-                  Target &tg, const rf_context_flags *fl) {
-    if (!vp || !fl) return RF_ERR_BAD_ARG;
+// One job of a frame: a target, its context flags and viewport, and the
+// draws rendered into it in order.
+struct JobIn {
+    const rf_draw *draws = nullptr;
+    uint32_t ndraws = 0;
+    const float *vp = nullptr;
+    Target *tg = nullptr;
+    const rf_context_flags *fl = nullptr;
+};
+
+// Host-side counts of one job (render.rs:152-155) and its slot among the
+// jobs that reach the GPU (-1: no triangles).
+struct JobHost {
+    uint64_t calls = 0, prims_i = 0, verts_i = 0;
+    int32_t slot = -1;
+};
+
+bool flags_ok(const rf_context_flags *fl) {
+    return fl && fl->depth_test >= RF_DEPTH_NONE && fl->depth_test <= RF_DEPTH_GREATER &&
+           fl->face_cull >= RF_CULL_NONE && fl->face_cull <= RF_CULL_FRONT;
+}
+
+void graphs_drop(rf_ctx *ctx) {
+    for (GraphEntry &g : ctx->gcache) cudaGraphExecDestroy(g.exec);
+    ctx->gcache.clear();
+}
+
+// Validates every draw of every job and fills ctx->hdraws / ctx->hjobs.
+// Nothing is queued on the GPU and no state changes on failure.
+rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<JobHost> &host,
+                     uint64_t &nv_out, uint64_t &nt_out) {
+    auto &hd = ctx->hdraws;
+    auto &hj = ctx->hjobs;
+    hd.clear();
+    hj.clear();
+    host.assign(nin, JobHost{});
+    uint64_t nv = 0, nt = 0;
+    uint64_t tiles = 0, mask_words = 0;
+    const uint32_t TW = ctx->tile_w;
+    for (uint32_t k = 0; k < nin; ++k) {
+        const JobIn &ji = in[k];
+        if (!ji.vp || !flags_ok(ji.fl) || !ji.tg || (ji.ndraws && !ji.draws)) return RF_ERR_BAD_ARG;
+        const size_t d0 = hd.size();
+        const uint64_t nt0 = nt, nv0 = nv;
+        for (uint32_t i = 0; i < ji.ndraws; ++i) {
+            const rf_draw &dr = ji.draws[i];
+            auto mit = ctx->meshes.find(dr.mesh);
+            if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+            const Mesh &m = mit->second;
+            if (dr.shader < RF_SHADER_FLAT || dr.shader > RF_SHADER_GOURAUD_SRGB) return RF_ERR_BAD_ARG;
+            if (m.nattr != nattr_for(dr.shader)) return RF_ERR_BAD_ARG;
+            DrawDev d{};
+            d.verts = m.verts;
+            d.idx = m.idx;
+            d.nverts = m.nverts;
+            d.ntri = m.ntri;
+            d.pos_dim = m.pos_dim;
+            d.nattr = m.nattr;
+            d.stride = m.pos_dim + m.nattr;
+            d.shader = dr.shader;
+            d.sampler = (int32_t)dr.uniforms.sampler;
+            d.flat_rgba = dr.uniforms.flat_rgba;
+            if (dr.shader == RF_SHADER_TEXTURED || dr.shader == RF_SHADER_TEX_GOURAUD) {
+                auto tit = ctx->textures.find(dr.uniforms.texture);
+                if (tit == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+                if (d.sampler < RF_SAMPLER_REPEAT_POT || d.sampler > RF_SAMPLER_ONCE) return RF_ERR_BAD_ARG;
+                if (d.sampler == RF_SAMPLER_REPEAT_POT && (!is_pot(tit->second.w) || !is_pot(tit->second.h)))
+                    return RF_ERR_NON_POT_TEXTURE;
+                d.tex = tit->second.texels;
+                d.tw = tit->second.w;
+                d.th = tit->second.h;
+            }
+            d.vert_base = (uint32_t)nv;
+            d.tri_base = (uint32_t)nt;
+            d.job = (uint32_t)hj.size();
+            memcpy(d.mvp, dr.uniforms.mvp, sizeof d.mvp);
+            nv += m.nverts;
+            nt += m.ntri;
+            if (nv > 0xFFFFFFF0ull || nt > 0x7FFFFFF0ull) return RF_ERR_BAD_ARG;
+            hd.push_back(d);
+        }
+        JobHost &h = host[k];
+        h.calls = ji.ndraws;
+        h.prims_i = nt - nt0;
+        h.verts_i = nv - nv0;
+        if (nt == nt0 || nv == nv0) {
+            // Nothing to draw: a pending clear stays pending for the next read.
+            hd.resize(d0);
+            nt = nt0;
+            nv = nv0;
+            continue;
+        }
+        const Target &tg = *ji.tg;
+        JobDev J{};
+        J.color = tg.color;
+        J.depth = tg.depth;
+        J.w = tg.w;
+        J.h = tg.h;
+        J.pixfmt = tg.fmt;
+        J.depth_test = ji.fl->depth_test;
+        J.color_write = ji.fl->color_write;
+        J.depth_write = ji.fl->depth_write;
+        J.face_cull = ji.fl->face_cull;
+        J.tiles_x = (tg.w + TW - 1) / TW;
+        J.tiles_y = (tg.h + RF_TILE_H - 1) / RF_TILE_H;
+        J.tile_base = (uint32_t)tiles;
+        J.tri_base = (uint32_t)nt0;
+        J.ntri = (uint32_t)(nt - nt0);
+        J.mask_words = (J.ntri + 31) / 32;
+        J.mask_base = mask_words;
+        J.clear_flags = tg.clear_flags;
+        J.clear_px = tg.clear_px;
+        J.clear_z = tg.clear_z;
+        memcpy(J.vp, ji.vp, sizeof J.vp);
+        tiles += (uint64_t)J.tiles_x * J.tiles_y;
+        mask_words += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
+        if (tiles > 0xFFFFFFF0ull) return RF_ERR_BAD_ARG;
+        h.slot = (int32_t)hj.size();
+        hj.push_back(J);
+    }
+    nv_out = nv;
+    nt_out = nt;
+    return RF_OK;
+}
+
+// One frame: the jobs of `in` (distinct targets), each with its draws in
+// order, as one pass of the pipeline over all of them.  per_job: kernels
+// count into per-job slots (ctx->jstats), folded into the running total at
+// the end of the pass; otherwise (a single job) straight into the total.
+rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
+                   std::vector<JobHost> &host) {
     rf_status st = init_stats(ctx);
     if (st) return st;
-    auto &hd = ctx->hdraws;
-    hd.clear();
-    hd.reserve(ndraws);
     uint64_t nv = 0, nt = 0;
-    for (uint32_t i = 0; i < ndraws; ++i) {
-        const rf_draw &dr = draws[i];
-        auto mit = ctx->meshes.find(dr.mesh);
-        if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
-        const Mesh &m = mit->second;
-        if (dr.shader < RF_SHADER_FLAT || dr.shader > RF_SHADER_GOURAUD_SRGB) return RF_ERR_BAD_ARG;
-        if (m.nattr != nattr_for(dr.shader)) return RF_ERR_BAD_ARG;
-        DrawDev d{};
-        d.verts = m.verts;
-        d.idx = m.idx;
-        d.nverts = m.nverts;
-        d.ntri = m.ntri;
-        d.pos_dim = m.pos_dim;
-        d.nattr = m.nattr;
-        d.stride = m.pos_dim + m.nattr;
-        d.shader = dr.shader;
-        d.sampler = (int32_t)dr.uniforms.sampler;
-        d.flat_rgba = dr.uniforms.flat_rgba;
-        if (dr.shader == RF_SHADER_TEXTURED || dr.shader == RF_SHADER_TEX_GOURAUD) {
-            auto tit = ctx->textures.find(dr.uniforms.texture);
-            if (tit == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
-            if (d.sampler < RF_SAMPLER_REPEAT_POT || d.sampler > RF_SAMPLER_ONCE) return RF_ERR_BAD_ARG;
-            if (d.sampler == RF_SAMPLER_REPEAT_POT && (!is_pot(tit->second.w) || !is_pot(tit->second.h)))
-                return RF_ERR_NON_POT_TEXTURE;
-            d.tex = tit->second.texels;
-            d.tw = tit->second.w;
-            d.th = tit->second.h;
-        }
-        d.vert_base = (uint32_t)nv;
-        d.tri_base = (uint32_t)nt;
-        d.job = 0;
-        memcpy(d.mvp, dr.uniforms.mvp, sizeof d.mvp);
-        nv += m.nverts;
-        nt += m.ntri;
-        hd.push_back(d);
+    if ((st = build_jobs(ctx, in, nin, host, nv, nt))) return st;
+    auto &hd = ctx->hdraws;
+    auto &hj = ctx->hjobs;
+    for (const JobHost &h : host) {
+        ctx->host_acc.calls += h.calls;
+        ctx->host_acc.prims_i += h.prims_i;
+        ctx->host_acc.verts_i += h.verts_i;
     }
-    if (nv > 0xFFFFFFF0ull || nt > 0x7FFFFFF0ull) return RF_ERR_BAD_ARG;
-    // Host-side counts (render.rs:152-155).
-    ctx->host_acc.calls += ndraws;
-    ctx->host_acc.prims_i += nt;
-    ctx->host_acc.verts_i += nv;
+    if (hj.empty()) return RF_OK;
+    const uint32_t nj = (uint32_t)hj.size();
+    if (nj > 1) per_job = true;
+    const JobDev &JL = hj.back();
+    const uint32_t ntiles = JL.tile_base + JL.tiles_x * JL.tiles_y;
+    const size_t mask_words = JL.mask_base + (size_t)JL.tiles_x * JL.tiles_y * JL.mask_words;
+    const uint32_t ndraws = (uint32_t)hd.size();
 
-    const uint32_t TW = ctx->tile_w;
-    JobDev J{};
-    J.color = tg.color;
-    J.depth = tg.depth;
-    J.w = tg.w;
-    J.h = tg.h;
-    J.pixfmt = tg.fmt;
-    J.depth_test = fl->depth_test;
-    J.color_write = fl->color_write;
-    J.depth_write = fl->depth_write;
-    J.face_cull = fl->face_cull;
-    J.tiles_x = (tg.w + TW - 1) / TW;
-    J.tiles_y = (tg.h + RF_TILE_H - 1) / RF_TILE_H;
-    J.tile_base = 0;
-    J.tri_base = 0;
-    J.ntri = (uint32_t)nt;
-    J.mask_words = (uint32_t)((nt + 31) / 32);
-    J.mask_base = 0;
-    J.clear_flags = tg.clear_flags;
-    J.clear_px = tg.clear_px;
-    J.clear_z = tg.clear_z;
-    memcpy(J.vp, vp, sizeof J.vp);
-    const uint32_t ntiles = J.tiles_x * J.tiles_y;
-    const size_t mask_words = (size_t)ntiles * J.mask_words;
-
-    if (nt == 0 || nv == 0) {
-        // Nothing to draw; a pending clear still lands on the next read.
-        return RF_OK;
-    }
     if ((st = ensure(ctx, ctx->draws, hd.size() * sizeof(DrawDev)))) return st;
-    if ((st = ensure(ctx, ctx->jobs, sizeof(JobDev)))) return st;
+    if ((st = ensure(ctx, ctx->jobs, hj.size() * sizeof(JobDev)))) return st;
+    if (per_job && (st = ensure(ctx, ctx->jstats, hj.size() * sizeof(StatsDev)))) return st;
     if ((st = ensure(ctx, ctx->cpos, nv * sizeof(float4)))) return st;
     if ((st = ensure(ctx, ctx->coc, nv))) return st;
     if ((st = ensure(ctx, ctx->tcnt, nt * 4))) return st;
@@ -279,6 +372,20 @@ rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const floa
     if ((st = ensure(ctx, ctx->rows, ctx->rows_cap * 4))) return st;
 
     cudaStream_t s = ctx->stream;
+    const uint32_t TW = ctx->tile_w;
+    int kind = hd[0].shader;
+    for (const DrawDev &d : hd)
+        if (d.shader != kind) kind = RF_K_ANY;
+    bool fast = true;
+    for (const JobDev &J : hj)
+        fast = fast && J.depth && J.depth_test == RF_DEPTH_LESS && J.color_write && J.depth_write;
+
+    // Per-frame parameters travel as data (draws, jobs); the launch sequence
+    // below depends only on the sizes, so it is replayed as a CUDA graph when
+    // a frame of the same shape comes again.
+    CK(cudaMemcpyAsync(ctx->draws.p, hd.data(), hd.size() * sizeof(DrawDev), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->jobs.p, hj.data(), hj.size() * sizeof(JobDev), cudaMemcpyHostToDevice, s));
+
     std::vector<cudaEvent_t> ev;
     if (ctx->timing) {
         for (int i = 0; i <= RF_STAGE_N; ++i) {
@@ -292,52 +399,93 @@ rf_status run_job(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws, const floa
             ev.push_back(e);
         }
     }
-    auto mark = [&](int i) -> cudaError_t {
-        return ctx->timing ? cudaEventRecord(ev[i], s) : cudaSuccess;
-    };
-    CK(cudaMemcpyAsync(ctx->draws.p, hd.data(), hd.size() * sizeof(DrawDev), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->jobs.p, &J, sizeof J, cudaMemcpyHostToDevice, s));
     uint32_t *counters = P<uint32_t>(ctx->counters);
-    CK(cudaMemsetAsync(counters + RF_CNT_POOL, 0, 4, s));
-    CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
-    CK(cudaMemsetAsync(ctx->mask.p, 0, mask_words * 4, s));
+    StatsDev *kst = per_job ? P<StatsDev>(ctx->jstats) : P<StatsDev>(ctx->stats);
     const DrawDev *dd = P<DrawDev>(ctx->draws);
     const JobDev *jd = P<JobDev>(ctx->jobs);
-    CK(mark(RF_STAGE_VERTEX));
-    CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
-                          ctx->nsm, s));
-    CK(mark(RF_STAGE_CLIP));
-    CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
-                        P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
-                        pool_cap, counters, ctx->nsm, s));
-    CK(mark(RF_STAGE_SCAN));
-    CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
-                        P<uint32_t>(ctx->scan), counters + RF_CNT_PRIMS, s));
-    CK(mark(RF_STAGE_SETUP));
-    CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
-                         P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
-                         P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), counters + RF_CNT_PRIMS,
-                         P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
-                         P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
-                         P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
-                         P<uint32_t>(ctx->mask), P<StatsDev>(ctx->stats), counters, ctx->nsm, s));
+    auto enqueue = [&](bool marks) -> rf_status {
+        auto mark = [&](int i) -> cudaError_t { return marks ? cudaEventRecord(ev[i], s) : cudaSuccess; };
+        CK(cudaMemsetAsync(counters + RF_CNT_POOL, 0, 4, s));
+        CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
+        CK(cudaMemsetAsync(ctx->mask.p, 0, mask_words * 4, s));
+        if (per_job) CK(cudaMemsetAsync(kst, 0, nj * sizeof(StatsDev), s));
+        CK(mark(RF_STAGE_VERTEX));
+        CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                              ctx->nsm, s));
+        CK(mark(RF_STAGE_CLIP));
+        CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                            P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
+                            pool_cap, counters, ctx->nsm, s));
+        CK(mark(RF_STAGE_SCAN));
+        CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
+                            P<uint32_t>(ctx->scan), counters + RF_CNT_PRIMS, s));
+        CK(mark(RF_STAGE_SETUP));
+        CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
+                             P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
+                             P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), counters + RF_CNT_PRIMS,
+                             P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
+                             P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
+                             P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
+                             P<uint32_t>(ctx->mask), kst, counters, ctx->nsm, s));
+        CK(mark(RF_STAGE_RASTER));
+        CK(rfk::launch_raster(TW, kind, fast, jd, nj, dd, P<PrimRec>(ctx->prims),
+                              P<RasterPrim>(ctx->rprims), P<uint32_t>(ctx->rows), P<uint32_t>(ctx->tcnt),
+                              P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles,
+                              counters + RF_CNT_QUEUE, kst, ctx->warps, ctx->nsm, s));
+        CK(mark(RF_STAGE_N));
+        if (per_job) CK(rfk::launch_stats_fold(kst, nj, P<StatsDev>(ctx->stats), s));
+        return RF_OK;
+    };
+
+    if (ctx->graphs && !ctx->timing) {
+        GraphKey key{};
+        const uint64_t kv[] = {ctx->gen, ndraws, nj, nv, nt, ntiles, mask_words, TW, ctx->warps,
+                               (uint64_t)(kind + 16), fast ? 1u : 0u, per_job ? 1u : 0u, ctx->rows_cap};
+        static_assert(sizeof kv == sizeof key.v, "graph key size");
+        memcpy(key.v, kv, sizeof kv);
+        GraphEntry *hit = nullptr;
+        for (GraphEntry &g : ctx->gcache)
+            if (g.key == key) hit = &g;
+        if (!hit) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            st = enqueue(false);
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (st) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+            cudaGraphExec_t ex = nullptr;
+            ce = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaGraphInstantiate");
+            if (ctx->gcache.size() >= RF_GRAPH_CACHE) {
+                size_t old = 0;
+                for (size_t i = 1; i < ctx->gcache.size(); ++i)
+                    if (ctx->gcache[i].used < ctx->gcache[old].used) old = i;
+                cudaGraphExecDestroy(ctx->gcache[old].exec);  // stream-ordered launches finish first
+                ctx->gcache.erase(ctx->gcache.begin() + old);
+            }
+            ctx->gcache.push_back(GraphEntry{key, ex, 0});
+            hit = &ctx->gcache.back();
+        }
+        hit->used = ++ctx->gclock;
+        CK(cudaGraphLaunch(hit->exec, s));
+        ctx->graph_launches += 1;
+    } else {
+        if ((st = enqueue(ctx->timing))) return st;
+    }
+    // vertex, clip, 3 scan, setup, 3 scan64, bin, raster (+ the stats fold)
+    ctx->kernels += 11 + (per_job ? 1 : 0);
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
         ctx->rows_evt_pending = true;
     }
-    CK(mark(RF_STAGE_RASTER));
-    int kind = hd[0].shader;
-    for (const DrawDev &d : hd)
-        if (d.shader != kind) kind = RF_K_ANY;
-    const bool fast = tg.depth && fl->depth_test == RF_DEPTH_LESS && fl->color_write && fl->depth_write;
-    CK(rfk::launch_raster(TW, kind, fast, jd, 1, dd, P<PrimRec>(ctx->prims),
-                          P<RasterPrim>(ctx->rprims), P<uint32_t>(ctx->rows), P<uint32_t>(ctx->tcnt),
-                          P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles,
-                          counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->warps, ctx->nsm, s));
-    CK(mark(RF_STAGE_N));
     if (ctx->timing) ctx->ev_pending.push_back(ev);
-    tg.clear_flags = 0;  // the raster pass wrote the pending clear
+    for (uint32_t k = 0; k < nin; ++k)
+        if (host[k].slot >= 0) in[k].tg->clear_flags = 0;  // the raster pass wrote the pending clear
     return RF_OK;
 }
 
@@ -345,6 +493,7 @@ rf_status flush_clear(rf_ctx *ctx, Target &tg) {
     if (!tg.clear_flags) return RF_OK;
     CK(rfk::launch_fill(tg.color, tg.depth, (size_t)tg.w * tg.h, tg.clear_px, tg.clear_z,
                         tg.clear_flags, ctx->nsm, ctx->stream));
+    ctx->kernels += 1;
     tg.clear_flags = 0;
     return RF_OK;
 }
@@ -421,10 +570,11 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     for (auto &kv : ctx->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); }
     for (auto &kv : ctx->textures) cudaFree(kv.second.texels);
     for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); }
+    graphs_drop(ctx);
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
-                      &ctx->rowtot, &ctx->rows, &ctx->rprims};
+                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->jstats};
     if (ctx->rows_need_host) cudaFreeHost(ctx->rows_need_host);
     if (ctx->rows_evt) cudaEventDestroy(ctx->rows_evt);
     for (DevBuf *b : bufs) cudaFree(b->p);
@@ -659,12 +809,212 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
     if (!ctx || (ndraws && !draws)) return RF_ERR_BAD_ARG;
     auto it = ctx->targets.find(target);
     if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
-    if (flags && (flags->depth_test < RF_DEPTH_NONE || flags->depth_test > RF_DEPTH_GREATER ||
-                  flags->face_cull < RF_CULL_NONE || flags->face_cull > RF_CULL_FRONT))
-        return RF_ERR_BAD_ARG;
-    rf_status st = run_job(ctx, draws, ndraws, viewport, it->second, flags);
+    JobIn ji;
+    ji.draws = draws;
+    ji.ndraws = ndraws;
+    ji.vp = viewport;
+    ji.tg = &it->second;
+    ji.fl = flags;
+    std::vector<JobHost> host;
+    rf_status st = run_jobs(ctx, &ji, 1, false, host);
     if (st) return st;
     return finish_call(ctx, stats);
+}
+
+rf_status rf_render_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, rf_stats *stats) {
+    if (!ctx || (njobs && !jobs)) return RF_ERR_BAD_ARG;
+    std::vector<JobIn> in(njobs);
+    std::vector<rf_target> seen(njobs);
+    for (uint32_t k = 0; k < njobs; ++k) {
+        auto it = ctx->targets.find(jobs[k].target);
+        if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+        in[k].draws = jobs[k].draws;
+        in[k].ndraws = jobs[k].ndraws;
+        in[k].vp = jobs[k].viewport;
+        in[k].tg = &it->second;
+        in[k].fl = &jobs[k].flags;
+        seen[k] = jobs[k].target;
+    }
+    std::sort(seen.begin(), seen.end());
+    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return RF_ERR_BAD_ARG;
+    std::vector<JobHost> host;
+    rf_status st = run_jobs(ctx, in.data(), njobs, true, host);
+    if (st) return st;
+    if (!stats) return RF_OK;
+    // Per-job stats: this batch's slots plus the host counts; the running
+    // total already holds them (folded on the device), so they are marked
+    // as handed out.
+    std::vector<StatsDev> js(ctx->hjobs.size());
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (!js.empty())
+        CK(cudaMemcpy(js.data(), ctx->jstats.p, js.size() * sizeof(StatsDev), cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < njobs; ++k) {
+        rf_stats o{};
+        o.calls = host[k].calls;
+        o.prims_i = host[k].prims_i;
+        o.verts_i = host[k].verts_i;
+        if (host[k].slot >= 0) {
+            const StatsDev &d = js[host[k].slot];
+            o.prims_o = d.prims_o;
+            o.verts_o = d.verts_o;
+            o.frags_i = d.frags_i;
+            o.frags_o = d.frags_o;
+            o.oob = d.oob;
+        }
+        stats[k] = o;
+        add_stats(ctx->taken, o);
+    }
+    return RF_OK;
+}
+
+rf_status rf_ctx_set_graphs(rf_ctx *ctx, int32_t enable) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    ctx->graphs = enable != 0;
+    if (!ctx->graphs) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        graphs_drop(ctx);
+    }
+    return RF_OK;
+}
+
+rf_status rf_ctx_counts(rf_ctx *ctx, uint64_t *kernels, uint64_t *graph_launches,
+                        uint32_t *graphs_cached) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    if (kernels) *kernels = ctx->kernels;
+    if (graph_launches) *graph_launches = ctx->graph_launches;
+    if (graphs_cached) *graphs_cached = (uint32_t)ctx->gcache.size();
+    return RF_OK;
+}
+
+rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint32_t reps,
+                          uint32_t *tile_w, uint32_t *warps, float *best_ms) {
+    if (!ctx || !jobs || !njobs) return RF_ERR_BAD_ARG;
+    if (reps == 0) reps = 3;
+    // Snapshot every target (pixels and pending clear) so each trial starts
+    // from the same state and the call leaves the targets as they were.
+    struct Snap {
+        Target *tg;
+        uint32_t *color = nullptr;
+        float *depth = nullptr;
+        uint32_t clear_flags;
+    };
+    std::vector<Snap> snaps;
+    std::vector<rf_target> handles;
+    for (uint32_t k = 0; k < njobs; ++k) {
+        auto it = ctx->targets.find(jobs[k].target);
+        if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+        handles.push_back(jobs[k].target);
+    }
+    std::sort(handles.begin(), handles.end());
+    if (std::adjacent_find(handles.begin(), handles.end()) != handles.end()) return RF_ERR_BAD_ARG;
+    rf_stats before{};
+    rf_status st = read_totals(ctx, before);
+    if (st) return st;
+    const uint32_t tw0 = ctx->tile_w, wp0 = ctx->warps;
+    const bool timing0 = ctx->timing;
+    ctx->timing = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        for (Snap &sn : snaps) {
+            cudaFree(sn.color);
+            cudaFree(sn.depth);
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        ctx->timing = timing0;
+    };
+    auto restore = [&]() -> cudaError_t {
+        for (Snap &sn : snaps) {
+            const size_t n = (size_t)sn.tg->w * sn.tg->h * 4;
+            cudaError_t e = cudaMemcpyAsync(sn.tg->color, sn.color, n, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (e == cudaSuccess && sn.depth)
+                e = cudaMemcpyAsync(sn.tg->depth, sn.depth, n, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (e != cudaSuccess) return e;
+            sn.tg->clear_flags = sn.clear_flags;
+        }
+        return cudaSuccess;
+    };
+    cudaError_t ce = cudaSuccess;
+    for (uint32_t k = 0; k < njobs && ce == cudaSuccess; ++k) {
+        Snap sn;
+        sn.tg = &ctx->targets.find(jobs[k].target)->second;
+        sn.clear_flags = sn.tg->clear_flags;
+        const size_t n = (size_t)sn.tg->w * sn.tg->h * 4;
+        ce = cudaMalloc(&sn.color, n);
+        if (ce == cudaSuccess && sn.tg->depth) ce = cudaMalloc(&sn.depth, n);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(sn.color, sn.tg->color, n, cudaMemcpyDeviceToDevice, ctx->stream);
+        if (ce == cudaSuccess && sn.depth)
+            ce = cudaMemcpyAsync(sn.depth, sn.tg->depth, n, cudaMemcpyDeviceToDevice, ctx->stream);
+        snaps.push_back(sn);
+    }
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, ce, "autotune setup");
+    }
+    static const uint32_t TWS[] = {8, 16, 32, 64};
+    static const uint32_t WPS[] = {4, 8};
+    float best = -1.0f;
+    uint32_t btw = tw0, bwp = wp0;
+    for (uint32_t tw : TWS) {
+        for (uint32_t wp : WPS) {
+            ctx->tile_w = tw;
+            ctx->warps = wp;
+            float tmin = -1.0f;
+            for (uint32_t r = 0; r <= reps && st == RF_OK; ++r) {  // r == 0: warm-up
+                if ((ce = restore()) != cudaSuccess) break;
+                if ((ce = cudaEventRecord(e0, ctx->stream)) != cudaSuccess) break;
+                st = rf_render_batch(ctx, jobs, njobs, nullptr);
+                if (st) break;
+                if ((ce = cudaEventRecord(e1, ctx->stream)) != cudaSuccess) break;
+                if ((ce = cudaEventSynchronize(e1)) != cudaSuccess) break;
+                float ms = 0.0f;
+                if ((ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) break;
+                if (r > 0 && (tmin < 0.0f || ms < tmin)) tmin = ms;
+            }
+            if (st || ce != cudaSuccess) break;
+            if (best < 0.0f || tmin < best) {
+                best = tmin;
+                btw = tw;
+                bwp = wp;
+            }
+        }
+        if (st || ce != cudaSuccess) break;
+    }
+    if (ce == cudaSuccess && !st) ce = restore();
+    if (ce == cudaSuccess && !st) ce = cudaStreamSynchronize(ctx->stream);
+    rf_stats after{};
+    if (ce == cudaSuccess && !st) st = read_totals(ctx, after);
+    cleanup();
+    if (ce != cudaSuccess) {
+        ctx->tile_w = tw0;
+        ctx->warps = wp0;
+        return cuda_fail(ctx, ce, "autotune");
+    }
+    if (st) {
+        ctx->tile_w = tw0;
+        ctx->warps = wp0;
+        return st;
+    }
+    // The trial renders are not the caller's: hide their stats.
+    rf_stats d{};
+    d.calls = after.calls - before.calls;
+    d.prims_i = after.prims_i - before.prims_i;
+    d.prims_o = after.prims_o - before.prims_o;
+    d.verts_i = after.verts_i - before.verts_i;
+    d.verts_o = after.verts_o - before.verts_o;
+    d.frags_i = after.frags_i - before.frags_i;
+    d.frags_o = after.frags_o - before.frags_o;
+    d.oob = after.oob - before.oob;
+    add_stats(ctx->taken, d);
+    ctx->tile_w = btw;
+    ctx->warps = bwp;
+    if (tile_w) *tile_w = btw;
+    if (warps) *warps = bwp;
+    if (best_ms) *best_ms = best;
+    return RF_OK;
 }
 
 }  // extern "C"

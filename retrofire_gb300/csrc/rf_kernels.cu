@@ -926,6 +926,45 @@ cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jo
     }
 }
 
+// Per-job stats of a batch folded into the context's running total.  One
+// block; stream order makes the plain read-modify-write of *total safe.
+__global__ void __launch_bounds__(256) k_stats_fold(const StatsDev *__restrict__ js, uint32_t n,
+                                                    StatsDev *__restrict__ total) {
+    __shared__ unsigned long long part[5][8];
+    unsigned long long a[5] = {0, 0, 0, 0, 0};
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+        a[0] += js[j].prims_o;
+        a[1] += js[j].verts_o;
+        a[2] += js[j].frags_i;
+        a[3] += js[j].frags_o;
+        a[4] += js[j].oob;
+    }
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[f] += __shfl_xor_sync(0xFFFFFFFFu, a[f], o);
+        if (lane == 0) part[f][w] = a[f];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t[5] = {0, 0, 0, 0, 0};
+        for (uint32_t i = 0; i < blockDim.x / 32; ++i)
+            for (int f = 0; f < 5; ++f) t[f] += part[f][i];
+        total->prims_o += t[0];
+        total->verts_o += t[1];
+        total->frags_i += t[2];
+        total->frags_o += t[3];
+        total->oob += t[4];
+    }
+}
+
+cudaError_t launch_stats_fold(const StatsDev *js, uint32_t n, StatsDev *total, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_stats_fold<<<1, 256, 0, s>>>(js, n, total);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fill(uint32_t *color, float *depth, size_t n, uint32_t px, float z,
                         uint32_t flags, int nsm, cudaStream_t s) {
     if (n == 0 || flags == 0) return cudaSuccess;

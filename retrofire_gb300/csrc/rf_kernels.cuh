@@ -90,6 +90,8 @@ RF_DECL_RASTER_TW(64)
 #undef RF_DECL_RASTER_TW
 cudaError_t launch_fill(uint32_t *color, float *depth, size_t n, uint32_t px, float z,
                         uint32_t flags, int nsm, cudaStream_t s);
+// Adds the n per-job stats slots js[0..n) into *total (one block).
+cudaError_t launch_stats_fold(const StatsDev *js, uint32_t n, StatsDev *total, cudaStream_t s);
 }  // namespace rfk
 
 #endif

@@ -169,3 +169,33 @@ def instanced_cubes(ninst=10_000, w=1920, h=1080, seed=3, tex_size=1024):
     verts, faces = cube_mesh(1.0, "col_uv")
     return dict(verts=verts, faces=faces, tex=noise_texture(tex_size, seed + 100), mvps=mvps,
                 vp=mat.viewport(0, h, w, 0), w=w, h=h)
+
+
+def batch_scenes(nscenes=256, seed=4, min_tris=12, max_tris=200_000, wmin=64, wmax=1920,
+                 hmin=64, hmax=1080):
+    """Uneven batch of independent scenes: target W and H log-uniform in
+    [wmin, wmax] x [hmin, hmax], triangle count log-uniform in [min_tris,
+    max_tris], and by coin flip either the fill-stress recipe (Gouraud
+    clip-space triangles; the area range scaled by the target's share of a
+    1920x1080 frame) or the instanced-cube recipe (tex x Gouraud, one draw
+    per cube, triangle count / 12 cubes, texture 64^2..1024^2).
+
+    Returns a list of dicts with kind ("fill" | "cubes"), w, h, vp and the
+    fields of fill_stress / instanced_cubes."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nscenes):
+        w = int(round(np.exp(rng.uniform(np.log(wmin), np.log(wmax)))))
+        h = int(round(np.exp(rng.uniform(np.log(hmin), np.log(hmax)))))
+        t = int(round(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris)))))
+        s = int(rng.integers(1, 1 << 30))
+        if rng.random() < 0.5:
+            amax = max(4.0, 1e4 * (w * h) / (1920.0 * 1080.0))
+            sc = fill_stress(ntri=max(1, t), w=w, h=h, seed=s, amax=amax)
+            sc["kind"] = "fill"
+        else:
+            tex = 1 << int(rng.integers(6, 11))
+            sc = instanced_cubes(ninst=max(1, t // 12), w=w, h=h, seed=s, tex_size=tex)
+            sc["kind"] = "cubes"
+        out.append(sc)
+    return out
