@@ -105,6 +105,9 @@ typedef struct {
  * Replaces the reference's implicit single thread (render.rs:134). */
 rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out);
 rf_status rf_ctx_destroy(rf_ctx *ctx);
+/* The CUDA device the context was created on (the caller's current device
+ * at rf_ctx_create). */
+rf_status rf_ctx_device(rf_ctx *ctx, int32_t *device);
 /* Waits for all work queued on the context's stream. */
 rf_status rf_ctx_sync(rf_ctx *ctx);
 /* Adds the stats of every render since the last call into *out (and syncs). */
@@ -136,6 +139,8 @@ rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint3
 /* Replaces the contents of a mesh with arrays of the same sizes (an
  * animated or re-submitted mesh without reallocation). */
 rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx);
+/* Sizes of a mesh; NULL pointers are skipped. */
+rf_status rf_mesh_info(rf_ctx *ctx, rf_mesh mesh, uint32_t *nverts, uint32_t *ntri, uint32_t *nattr);
 rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh);
 /* rgba: w*h texels, Color4 bytes r,g,b,a little-endian, row-major
  * (Texture<Buf2<Color4>>, tex.rs:33-37). */
@@ -247,6 +252,72 @@ rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint32_t pos_di
                             int32_t pixfmt, const rf_context_flags *flags,
                             const uint32_t *clear_rgba, const float *depth_clear,
                             void *cuda_stream, rf_stats *stats);
+
+/* ---- serving loop -----------------------------------------------------
+ * No counterpart in the reference, which renders one frame per call on
+ * the caller's thread (render.rs:134).  A server takes over an rf_ctx
+ * whose meshes and textures are already uploaded and runs a worker thread
+ * on it.  Any thread submits requests: a scene (draws on the context's
+ * meshes and textures, a viewport, context flags), a target size and
+ * format, the Frame::clear values and host buffers for the image.
+ *
+ * Admission: each request is charged an estimate of the device memory it
+ * needs (its target plus RF_SERVE_BYTES_PER_TRI per input triangle and
+ * RF_SERVE_BYTES_PER_VERT per vertex of scratch); a request whose estimate
+ * alone exceeds the budget is refused at submit (RF_ERR_OVER_BUDGET).
+ * Continuous batching: the worker takes, in arrival order, every queued
+ * request that fits the budget (at most max_batch), renders them with one
+ * rf_render_batch into pooled targets, copies each image into its host
+ * buffers and completes the requests; requests that arrive meanwhile form
+ * the next batch.  A request's image and stats equal rf_render_draws of
+ * its scene alone on a cleared target, whatever batch it lands in.  A
+ * request that fails validation (bad handle, bad argument) fails alone.
+ *
+ * While a server runs, the context belongs to it: the caller makes no
+ * other call on that context until rf_server_destroy, which drains the
+ * queue, joins the worker and frees the pooled targets (the context and
+ * its meshes and textures stay the caller's). */
+#define RF_SERVE_BYTES_PER_TRI 5632u
+#define RF_SERVE_BYTES_PER_VERT 24u
+typedef struct rf_server rf_server;
+typedef struct {
+    uint64_t hbm_budget_bytes; /* 0: 64 GiB */
+    uint32_t max_batch;        /* 0: 256 */
+    uint32_t reserved_;
+} rf_server_config;
+typedef struct {
+    uint32_t ndraws;
+    const rf_draw *draws;      /* copied at submit */
+    float viewport[16];
+    rf_context_flags flags;
+    uint32_t w, h;
+    int32_t pixfmt;
+    int32_t has_depth;
+    uint32_t clear_rgba;       /* Color4 bytes r,g,b,a (Context::color_clear) */
+    float depth_clear;         /* Context::depth_clear; the buffer gets 1/x */
+    uint32_t *color_out;       /* host, w*h pixels, or NULL */
+    float *depth_out;          /* host, w*h, or NULL (ignored without depth) */
+} rf_request;
+typedef struct {
+    int32_t status;            /* the request's own status */
+    uint32_t batch_size;       /* requests in the batch it was rendered in */
+    uint64_t batch_id;
+    double queue_ms;           /* submit -> its batch started */
+    double render_ms;          /* its batch: start -> rendered (GPU done) */
+    double total_ms;           /* submit -> image in the host buffers */
+    rf_stats stats;
+} rf_result;
+rf_status rf_server_create(rf_ctx *ctx, const rf_server_config *cfg, rf_server **out);
+/* Queues a request; *ticket identifies it for rf_server_wait.  The host
+ * buffers must stay valid until the request completes. */
+rf_status rf_server_submit(rf_server *srv, const rf_request *req, uint64_t *ticket);
+/* Waits up to timeout_ms (UINT32_MAX: no limit) for a request; RF_OK and
+ * its result, RF_ERR_TIMEOUT if still pending, RF_ERR_BAD_ARG for a ticket
+ * that was never issued or was already collected. */
+rf_status rf_server_wait(rf_server *srv, uint64_t ticket, uint32_t timeout_ms, rf_result *out);
+/* Batches rendered, requests completed, requests queued right now. */
+rf_status rf_server_counts(rf_server *srv, uint64_t *batches, uint64_t *completed, uint64_t *queued);
+rf_status rf_server_destroy(rf_server *srv);
 
 #ifdef __cplusplus
 }

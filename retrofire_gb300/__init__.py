@@ -73,6 +73,24 @@ class Job(C.Structure):
                 ("viewport", C.c_float * 16), ("flags", Flags)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch", C.c_uint32),
+                ("reserved_", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("ndraws", C.c_uint32), ("draws", C.POINTER(Draw)), ("viewport", C.c_float * 16),
+                ("flags", Flags), ("w", C.c_uint32), ("h", C.c_uint32), ("pixfmt", C.c_int32),
+                ("has_depth", C.c_int32), ("clear_rgba", C.c_uint32), ("depth_clear", C.c_float),
+                ("color_out", C.POINTER(C.c_uint32)), ("depth_out", C.POINTER(C.c_float))]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_uint32), ("batch_id", C.c_uint64),
+                ("queue_ms", C.c_double), ("render_ms", C.c_double), ("total_ms", C.c_double),
+                ("stats", CStats)]
+
+
 # Exported symbols of include/rfgpu.h with their ctypes signatures.
 _P = C.c_void_p
 _SIGS = {
@@ -101,6 +119,14 @@ _SIGS = {
     "rf_render_draws": [_P, C.POINTER(Draw), C.c_uint32, C.POINTER(C.c_float), C.c_uint64,
                         C.POINTER(Flags), C.POINTER(CStats)],
     "rf_render_batch": [_P, C.POINTER(Job), C.c_uint32, C.POINTER(CStats)],
+    "rf_ctx_device": [_P, C.POINTER(C.c_int32)],
+    "rf_mesh_info": [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                     C.POINTER(C.c_uint32)],
+    "rf_server_create": [_P, C.POINTER(ServerConfig), C.POINTER(_P)],
+    "rf_server_submit": [_P, C.POINTER(Request), C.POINTER(C.c_uint64)],
+    "rf_server_wait": [_P, C.c_uint64, C.c_uint32, C.POINTER(Result)],
+    "rf_server_counts": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
+    "rf_server_destroy": [_P],
     "rf_ctx_set_graphs": [_P, C.c_int32],
     "rf_ctx_counts": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)],
     "rf_ctx_autotune": [_P, C.POINTER(Job), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
@@ -485,3 +511,78 @@ def autotune(scenes, reps=3, device=None):
                                  C.byref(ms)), "rf_ctx_autotune")
     del keep
     return tw.value, wp.value, ms.value
+
+
+class Server:
+    """rf_server: a worker thread that owns the device context and renders
+    queued requests in continuous batches under a device-memory budget.
+    While it runs, make no other call on that Device."""
+
+    WAIT_FOREVER = 0xFFFFFFFF
+
+    def __init__(self, device, hbm_budget_bytes=0, max_batch=0):
+        self.dev = device
+        cfg = ServerConfig(hbm_budget_bytes, max_batch, 0)
+        p = _P()
+        _check(lib().rf_server_create(device.ptr, C.byref(cfg), C.byref(p)), "rf_server_create")
+        self.ptr = p
+        self._keep = {}
+
+    def submit(self, draws, to_screen, w, h, ctx=None, pixfmt=ARGB8888, depth=True,
+               color_out=None, depth_out=None):
+        """Queue a scene; returns a ticket.  draws: list of (Mesh, Shader,
+        mvp).  color_out / depth_out: (h, w) uint32 / float32 host arrays
+        that receive the image (allocated here when None)."""
+        ctx = ctx or Context()
+        arr = (Draw * max(1, len(draws)))()
+        for i, (mesh, shader, mvp) in enumerate(draws):
+            arr[i].mesh = mesh.handle
+            arr[i].shader = shader.kind
+            arr[i].uniforms = shader.uniforms(mvp)
+        if color_out is None:
+            color_out = np.empty((h, w), np.uint32)
+        if depth and depth_out is None:
+            depth_out = np.empty((h, w), np.float32)
+        q = Request()
+        q.ndraws = len(draws)
+        q.draws = C.cast(arr, C.POINTER(Draw))
+        q.viewport[:] = [float(x) for x in np.asarray(to_screen, np.float32).reshape(-1)]
+        q.flags = ctx.flags()
+        q.w, q.h, q.pixfmt, q.has_depth = w, h, pixfmt, int(bool(depth))
+        cc = 0xFF000000 if ctx.color_clear is None else ctx.color_clear
+        q.clear_rgba = cc
+        q.depth_clear = float("inf") if ctx.depth_clear is None else ctx.depth_clear
+        q.color_out = _u32p(color_out)
+        q.depth_out = _fp(depth_out) if depth else None
+        t = C.c_uint64()
+        _check(lib().rf_server_submit(self.ptr, C.byref(q), C.byref(t)), "rf_server_submit")
+        self._keep[t.value] = (color_out, depth_out if depth else None)
+        return t.value
+
+    def wait(self, ticket, timeout_ms=WAIT_FOREVER):
+        """(color, depth, result dict) of a request; raises RfError with
+        code 7 on timeout.  result["status"] is the request's own status."""
+        r = Result()
+        _check(lib().rf_server_wait(self.ptr, ticket, timeout_ms, C.byref(r)), "rf_server_wait")
+        col, dep = self._keep.pop(ticket)
+        res = {"status": r.status, "batch_size": r.batch_size, "batch_id": r.batch_id,
+               "queue_ms": r.queue_ms, "render_ms": r.render_ms, "total_ms": r.total_ms,
+               "stats": Stats.from_c(r.stats)}
+        return col, dep, res
+
+    def counts(self):
+        b, c, q = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().rf_server_counts(self.ptr, C.byref(b), C.byref(c), C.byref(q)),
+               "rf_server_counts")
+        return {"batches": b.value, "completed": c.value, "queued": q.value}
+
+    def close(self):
+        if self.ptr:
+            lib().rf_server_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -63,6 +63,7 @@ struct rf_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int nsm = 1;
+    int device = 0;
     uint32_t tile_w = 32, warps = 4;
     uint64_t next_handle = 1;
     std::unordered_map<uint64_t, Mesh> meshes;
@@ -549,6 +550,7 @@ rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out) {
     if (!ctx) return RF_ERR_OOM;
     int dev = 0;
     cudaGetDevice(&dev);
+    ctx->device = dev;
     cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, dev);
     if (cuda_stream) {
         ctx->stream = (cudaStream_t)cuda_stream;
@@ -583,6 +585,12 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     for (cudaEvent_t e : ctx->ev_free) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+    return RF_OK;
+}
+
+rf_status rf_ctx_device(rf_ctx *ctx, int32_t *device) {
+    if (!ctx || !device) return RF_ERR_BAD_ARG;
+    *device = ctx->device;
     return RF_OK;
 }
 
@@ -673,6 +681,16 @@ rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const ui
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return RF_OK;
+}
+
+rf_status rf_mesh_info(rf_ctx *ctx, rf_mesh mesh, uint32_t *nverts, uint32_t *ntri, uint32_t *nattr) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->meshes.find(mesh);
+    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    if (nverts) *nverts = it->second.nverts;
+    if (ntri) *ntri = it->second.ntri;
+    if (nattr) *nattr = it->second.nattr;
     return RF_OK;
 }
 

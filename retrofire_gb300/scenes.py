@@ -199,3 +199,70 @@ def batch_scenes(nscenes=256, seed=4, min_tris=12, max_tris=200_000, wmin=64, wm
             sc["kind"] = "cubes"
         out.append(sc)
     return out
+
+
+def grid_mesh(n, seed=0, attrs="col"):
+    """Heightfield over [-1, 1]^2 in x/z: (n+1)^2 vertices, 2 n^2 triangles,
+    y a seeded sum of four sine waves, colour from height.  attrs "col"
+    (Gouraud, 3 attributes) or "col_uv" (tex x Gouraud: colour, then UV
+    repeating 4 times across the grid).  Returns (verts, faces)."""
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(-1.0, 1.0, n + 1)
+    X, Z = np.meshgrid(xs, xs)
+    k = rng.uniform(1.0, 4.0, size=(4, 2))
+    ph = rng.uniform(0.0, 2 * np.pi, size=4)
+    Y = sum(np.sin(k[i, 0] * np.pi * X + k[i, 1] * np.pi * Z + ph[i]) for i in range(4)) * 0.04
+    t = (Y - Y.min()) / max(1e-9, float(Y.max() - Y.min()))
+    col = np.stack([0.2 + 0.6 * t, 0.5 + 0.3 * (1 - t), 0.3 + 0.2 * np.cos(3 * t)], -1)
+    cols = [X, Y, Z, col[..., 0], col[..., 1], col[..., 2]]
+    if attrs == "col_uv":
+        cols += [(X + 1.0) * 2.0, (Z + 1.0) * 2.0]
+    verts = np.stack(cols, -1).reshape(-1, len(cols)).astype(f32)
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    v00 = (i * (n + 1) + j).reshape(-1)
+    v01, v10 = v00 + 1, v00 + n + 1
+    v11 = v10 + 1
+    faces = np.concatenate([np.stack([v00, v11, v01], -1), np.stack([v00, v10, v11], -1)])
+    return verts, faces.astype(np.uint32)
+
+
+# Preloaded mesh set of the serving workload: (name, shader, mesh builder).
+SERVING_MESHES = (
+    ("cube12", "textured", lambda: cube_mesh(1.6, "uv")),
+    ("grid128", "gouraud", lambda: grid_mesh(8, 1)),
+    ("grid2k", "tex_gouraud", lambda: grid_mesh(32, 2, "col_uv")),
+    ("grid33k", "gouraud", lambda: grid_mesh(128, 3)),
+    ("grid500k", "tex_gouraud", lambda: grid_mesh(500, 4, "col_uv")),
+)
+SERVING_RESOLUTIONS = ((320, 240, 0.4), (640, 480, 0.3), (1280, 720, 0.2), (1920, 1080, 0.1))
+
+
+def orbit_camera(seed, w, h, dist=(2.4, 3.6), pitch=(0.35, 1.0)):
+    """Per-request camera: yaw U[0, 2 pi), pitch and distance uniform in the
+    given ranges, looking at the origin; horizontal FOV 60 degrees, near /
+    far 0.1..100.  Returns the 4x4 view-projection matrix."""
+    rng = np.random.default_rng(seed)
+    yaw = rng.uniform(0.0, 2 * np.pi)
+    pt = rng.uniform(*pitch)
+    d = rng.uniform(*dist)
+    eye = [d * np.cos(pt) * np.sin(yaw), d * np.sin(pt), -d * np.cos(pt) * np.cos(yaw)]
+    aspect = f32(w) / f32(h)
+    proj = mat.perspective(mat.focal_ratio_horizontal(np.pi / 3.0), aspect, 0.1, 100.0)
+    return mat.then(_look_at(eye, [0.0, 0.0, 0.0]), proj)
+
+
+def serving_requests(n, rate, seed=5, meshes=SERVING_MESHES, resolutions=SERVING_RESOLUTIONS):
+    """n requests with Poisson arrivals at `rate` per second: dicts with
+    t (arrival offset, s), mesh (index into meshes), w, h, mvp, vp."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    p = np.array([r[2] for r in resolutions])
+    ri = rng.choice(len(resolutions), size=n, p=p / p.sum())
+    mi = rng.integers(0, len(meshes), size=n)
+    cs = rng.integers(1, 1 << 30, size=n)
+    out = []
+    for k in range(n):
+        w, h = resolutions[ri[k]][:2]
+        out.append(dict(t=float(t[k]), mesh=int(mi[k]), w=w, h=h,
+                        mvp=orbit_camera(int(cs[k]), w, h), vp=mat.viewport(0, h, w, 0)))
+    return out

@@ -63,3 +63,18 @@ def test_null_arguments_rejected(libpath):
     assert L.rf_ctx_create(None, None) == 2
     assert L.rf_ctx_destroy(None) == 2
     assert L.rf_render(None, 0, 0, None, None, 0, None, None) == 2
+
+
+def test_batch_and_server_null_arguments(libpath):
+    L = rf.lib()
+    assert L.rf_render_batch(None, None, 0, None) == 2
+    assert L.rf_ctx_autotune(None, None, 0, 1, None, None, None) == 2
+    assert L.rf_ctx_set_graphs(None, 1) == 2
+    assert L.rf_ctx_counts(None, None, None, None) == 2
+    assert L.rf_mesh_info(None, 1, None, None, None) == 2
+    p = C.c_void_p()
+    assert L.rf_server_create(None, None, C.byref(p)) == 2
+    assert L.rf_server_submit(None, None, None) == 2
+    assert L.rf_server_wait(None, 1, 0, None) == 2
+    assert L.rf_server_counts(None, None, None, None) == 2
+    assert L.rf_server_destroy(None) == 2
