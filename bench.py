@@ -344,6 +344,248 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+# ------------------------------------------------- further workloads ---
+#
+# --workload picks one of the reference's other configurations; each prints
+# one JSON line with the same keys as the default.  Not the default line.
+
+def _oracle_scene(sc):
+    """Renders one bench scene dict with the oracle; returns Stats."""
+    import numpy as np
+    from oracle import oracle as O
+    col = np.zeros((sc["h"], sc["w"]), np.uint32)
+    dep = np.zeros((sc["h"], sc["w"]), np.float32)
+    O.clear(col, dep)
+    ods = [O.make_draw(d["verts"], d["faces"], d["shader"], d["mvp"], pos_dim=d["pos_dim"],
+                       tex=d.get("tex")) for d in sc["draws"]]
+    return O.render(ods, sc["vp"], col, dep, {})
+
+
+def _oracle_scenes(args):
+    """Worker: (seconds, frags_i, n) of the oracle over the given scenes."""
+    sys.path.insert(0, ROOT)
+    from retrofire_gb300 import workloads
+    name, idx = args
+    scs = workloads.scenes_for(name)
+    fr = 0
+    t0 = time.perf_counter()
+    for i in idx:
+        fr += _oracle_scene(scs[i]).frags_i
+    return time.perf_counter() - t0, fr, len(idx)
+
+
+def cpu_sample(name, idx, workers):
+    """frags/s and items/s of the oracle over scenes `idx` of a workload."""
+    if workers == 1:
+        t, fr, n = _oracle_scenes((name, idx))
+        return fr / t, n / t, t
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    parts = [idx[k::workers] for k in range(workers)]
+    with ctx.Pool(workers) as pool:
+        pool.map(_oracle_scenes, [(name, [])] * workers)
+        t0 = time.perf_counter()
+        res = pool.map(_oracle_scenes, [(name, p) for p in parts])
+        wall = time.perf_counter() - t0
+    fr = sum(r[1] for r in res)
+    return fr / wall, len(idx) / wall, wall
+
+
+def device_time(dev, stream, step, steps, warmup, flush, local, stages=True):
+    import torch
+    for _ in range(warmup):
+        step()
+    dev.sync()
+    dev.stage_ms()
+    if stages:
+        dev.set_timing(True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    clocks = Clocks(local)
+    torch.cuda.synchronize()
+    k0 = dev.counts()["kernels"]
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            if flush is not None:
+                flush.fill_(i & 0xFF)
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = dev.counts()["kernels"] - k0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    stage, nfr = dev.stage_ms()
+    dev.set_timing(False)
+    return step_ms, {k: v / max(nfr, 1) for k, v in stage.items()}, launches, clk
+
+
+def run_workload(args):
+    """C1 cube / C3 cubes / C4 batch on one GPU (replicas for N > 1)."""
+    import numpy as np
+    import torch
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import workloads
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    name = args.workload
+    scs = workloads.scenes_for(name)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        idx = workloads.cpu_sample_indices(name)
+        fr, it, t = cpu_sample(name, idx, 1)
+        cpu = {"value": fr, "unit": "frags/s", "cores": 1, "kind": "port",
+               "items_per_s": it,
+               "sample": "%d of the workload's %d scenes, single thread, %.1f s"
+                         % (len(idx), len(scs), t)}
+    stream = torch.cuda.Stream()
+    dev = rf.Device(stream.cuda_stream)
+    if args.tile or args.warps:
+        dev.set_tiling(args.tile, args.warps)
+    objs = workloads.upload(scs, dev)
+    batch = objs["scenes"]
+    st = rf.render_batch(batch, device=dev)  # per-scene stats of one step
+    frags_i = sum(x.frags_i for x in st)
+    frags_o = sum(x.frags_o for x in st)
+    px = sum(sc["w"] * sc["h"] for sc in scs)
+    graphs = name == "cube"
+    if graphs:
+        dev.set_graphs(True)
+    flush = None if args.no_flush else torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        for tg in objs["targets"]:
+            tg.clear()
+        rf.render_batch(batch, device=dev, sync_stats=False)
+
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms, stage, launches, clk = device_time(dev, stream, step, args.steps, args.warmup,
+                                                flush, local, stages=not graphs)
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    e2e = None
+    if not args.no_e2e:
+        e2e = workloads.e2e(objs, dev, args.steps, max(1, args.warmup))
+        e2e["value"] = frags_i * args.steps * world / e2e.pop("seconds")
+        e2e["unit"] = "frags/s"
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        roof = None
+        if stage.get("raster"):
+            alg = 4 * frags_i + 8 * frags_o + 8 * px
+            ach = alg / (stage["raster"] / 1e3) / 1e9
+            roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak, "traffic": None, "kernel": "k_raster",
+                    "peak_kind": peak_kind, "alg_bytes_per_launch": alg}
+        line = {
+            "metric": METRIC, "value": frags_i * args.steps * world / (total_ms / 1e3),
+            "unit": "frags/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": dict(workloads.describe(name), graphs=graphs,
+                           l2="flushed between steps (512 MiB write)" if flush is not None
+                           else "not flushed"),
+            "items_per_s": len(scs) * args.steps * world / (total_ms / 1e3),
+            "frags_i_per_step": frags_i, "frags_o_per_step": frags_o,
+            "stage_ms_per_step": stage if not graphs else None,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches, "clocks": clk,
+        }
+        print(json.dumps(line))
+    workloads.close(objs)
+    dev.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_serve(args):
+    """C5: Poisson request stream through rf_server; requests/s and latency."""
+    import torch
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import scenes, serve
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = rf.Device()
+    ms = serve.MeshSet(dev)
+    lines = []
+    for rate in args.rates:
+        reqs = scenes.serving_requests(int(rate * args.duration), float(rate), seed=100 + int(rate))
+        srv = rf.Server(dev, hbm_budget_bytes=64 << 30)
+        serve.run_load(srv, ms, reqs[:40], realtime=False, depth=False)  # warm-up
+        clocks = Clocks(local)
+        clocks.start()
+        res, wall = serve.run_load(srv, ms, reqs, realtime=True, depth=False)
+        clk = clocks.stop()
+        s = serve.latency_summary(res)
+        lines.append((rate, len(reqs), wall, s, srv.counts(), clk))
+        srv.close()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        fr, it, t = cpu_sample("serve", list(range(60)), 1)
+        cpu = {"value": it, "unit": "requests/s", "cores": 1, "kind": "port",
+               "sample": "60 requests of the stream rendered by the oracle, single thread, %.1f s" % t}
+    if rank == 0:
+        rate, n, wall, s, c, clk = lines[-1]
+        h2d = 0
+        line = {"metric": "requests/s", "value": n / wall, "unit": "requests/s", "n_gpus": world,
+                "steps": n, "warmup": 40, "ms_per_step": 1e3 * wall / n, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded Poisson request stream)",
+                "config": {"workload": "serving_poisson", "rate_per_s": rate,
+                           "duration_s": args.duration, "hbm_budget_gb": 64,
+                           "meshes": [m[0] for m in scenes.SERVING_MESHES],
+                           "resolutions": scenes.SERVING_RESOLUTIONS,
+                           "readback": "colour to host per request"},
+                "latency_ms": {"p50": s["p50_ms"], "p99": s["p99_ms"]},
+                "per_rate": [{"rate": r, "served_per_s": nn / w, **ss, **cc}
+                             for r, nn, w, ss, cc, _ in lines],
+                "e2e": {"value": n / wall, "unit": "requests/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": None},
+                "cpu_baseline": cpu, "roofline": None, "gpu_launches": None, "clocks": clk}
+        print(json.dumps(line))
+    ms.close()
+    dev.close()
+
+
+def run_reference_workload(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as obuild
+    obuild.build()
+    sys.path.insert(0, ROOT)
+    from retrofire_gb300 import workloads
+    name = args.workload
+    cores = os.cpu_count() or 1
+    idx = workloads.cpu_sample_indices(name, cores)
+    times, frs, its = [], [], []
+    for i in range(args.warmup + args.steps):
+        fr, it, t = cpu_sample(name, idx, cores)
+        if i >= args.warmup:
+            times.append(t)
+            frs.append(fr)
+            its.append(it)
+    metric, unit = ("requests/s", "requests/s") if name == "serve" else (METRIC, "frags/s")
+    value = (sum(its) if name == "serve" else sum(frs)) / len(times)
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference", "config": workloads.describe(name),
+            "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port",
+                             "sample": "%d scenes per step over %d cores" % (len(idx), cores)},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,13 +598,27 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
     ap.add_argument("--no-flush", action="store_true", help="no L2 flush buffer (profiling)")
+    ap.add_argument("--workload", default="fill", choices=["fill", "cube", "cubes", "batch", "serve"],
+                    help="fill: the headline frame (default); cube: 640x480 textured cube "
+                         "(latency, CUDA graphs); cubes: 10k instanced cubes, one draw each; "
+                         "batch: 256 uneven scenes in one pass; serve: Poisson request stream")
+    ap.add_argument("--rates", type=float, nargs="+", default=[200.0, 1000.0, 2000.0])
+    ap.add_argument("--duration", type=float, default=2.0)
     args = ap.parse_args()
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "fill":
+            run_reference(args)
+        else:
+            run_reference_workload(args)
         return
     import __graft_entry__
     __graft_entry__.build()
-    run_gpu(args)
+    if args.workload == "fill":
+        run_gpu(args)
+    elif args.workload == "serve":
+        run_serve(args)
+    else:
+        run_workload(args)
 
 
 if __name__ == "__main__":

@@ -453,22 +453,47 @@ def render_draws(draws, to_screen, target, ctx=None, sync_stats=True):
 
 class Scene:
     """One job of a batch: a target, its Context flags and viewport, and the
-    render() calls into it, in order.  draws: list of (Mesh, Shader, mvp)."""
+    render() calls into it, in order.  draws: list of (Mesh, Shader, mvp).
+    The C draw records are built once, at first use; set_draws replaces
+    them (for a scene whose matrices change between frames)."""
 
     def __init__(self, target, draws, to_screen, ctx=None):
-        self.target, self.draws, self.ctx = target, list(draws), ctx or Context()
+        self.target, self.ctx = target, ctx or Context()
         self.to_screen = np.ascontiguousarray(to_screen, np.float32).reshape(-1)
+        self.set_draws(draws)
+
+    def set_draws(self, draws):
+        self.draws = list(draws)
+        self._arr = None
+
+    def _draw_array(self):
+        if self._arr is None:
+            arr = (Draw * max(1, len(self.draws)))()
+            if self.draws:
+                mvps = np.zeros((len(self.draws), 16), np.float32)
+                for i, (mesh, shader, mvp) in enumerate(self.draws):
+                    arr[i].mesh = mesh.handle
+                    arr[i].shader = shader.kind
+                    arr[i].uniforms = shader.uniforms(None)
+                    if mvp is not None:
+                        mvps[i] = np.asarray(mvp, np.float32).reshape(-1)
+                    else:
+                        mvps[i] = np.eye(4, dtype=np.float32).reshape(-1)
+                # the 16 mvp floats of every record in one strided copy
+                raw = np.ctypeslib.as_array(C.cast(arr, C.POINTER(C.c_uint8)),
+                                            (len(self.draws) * C.sizeof(Draw),))
+                rec = raw.reshape(len(self.draws), C.sizeof(Draw))
+                off = Draw.uniforms.offset + Uniforms.mvp.offset
+                rec[:, off:off + 64] = mvps.view(np.uint8).reshape(-1, 64)
+            self._arr = arr
+        return self._arr
 
 
 def _jobs(scenes):
     jobs = (Job * len(scenes))()
     keep = []
     for j, sc in zip(jobs, scenes):
-        arr = (Draw * max(1, len(sc.draws)))()
-        for i, (mesh, shader, mvp) in enumerate(sc.draws):
-            arr[i].mesh = mesh.handle
-            arr[i].shader = shader.kind
-            arr[i].uniforms = shader.uniforms(mvp)
+        arr = sc._draw_array()
         keep.append(arr)
         j.target = sc.target.handle
         j.ndraws = len(sc.draws)

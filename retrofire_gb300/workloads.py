@@ -1,0 +1,159 @@
+"""The measured workloads beyond the headline frame, as lists of scenes.
+
+A scene is a dict: w, h, vp (viewport matrix) and draws, each draw a dict of
+verts, faces, shader, mvp, pos_dim and tex (texels or None); draws that
+share a vertex array share one device mesh.
+
+  cube    640x480 textured cube, seed-drawn rotation (latency case)
+  cubes   1920x1080, 10,000 instanced tex x Gouraud cubes, one render()
+          call per instance (demos/src/bin/crates.rs:114-133 idiom)
+  batch   256 uneven independent scenes (scenes.batch_scenes)
+  serve   the first requests of the serving stream as scenes
+"""
+import functools
+import time
+
+import numpy as np
+
+from . import (GOURAUD, TEX_GOURAUD, TEXTURED, Framebuf, Mesh, Scene, Shader, Texture, scenes)
+
+
+def _draw(verts, faces, shader, mvp=None, pos_dim=3, tex=None):
+    return dict(verts=verts, faces=faces, shader=shader, mvp=mvp, pos_dim=pos_dim, tex=tex)
+
+
+def _from_batch_entry(sc):
+    if sc["kind"] == "fill":
+        draws = [_draw(sc["verts"], sc["faces"], GOURAUD, None, 4)]
+    else:
+        draws = [_draw(sc["verts"], sc["faces"], TEX_GOURAUD, m, 3, sc["tex"]) for m in sc["mvps"]]
+    return dict(w=sc["w"], h=sc["h"], vp=sc["vp"], draws=draws)
+
+
+@functools.lru_cache(maxsize=None)
+def scenes_for(name):
+    if name == "cube":
+        c = scenes.textured_cube(seed=1, w=640, h=480)
+        return [dict(w=640, h=480, vp=c["vp"],
+                     draws=[_draw(c["verts"], c["faces"], TEXTURED, c["mvp"], 3, c["tex"])])]
+    if name == "cubes":
+        s = scenes.instanced_cubes(ninst=10_000, w=1920, h=1080, seed=3, tex_size=1024)
+        s["kind"] = "cubes"
+        return [_from_batch_entry(s)]
+    if name == "batch":
+        return [_from_batch_entry(s) for s in scenes.batch_scenes(256, seed=4)]
+    if name == "serve":
+        built = [(sh, b()) for _, sh, b in scenes.SERVING_MESHES]
+        tex = scenes.noise_texture(256, 9)
+        kinds = {"textured": TEXTURED, "gouraud": GOURAUD, "tex_gouraud": TEX_GOURAUD}
+        out = []
+        for r in scenes.serving_requests(60, 2000.0, seed=2100):
+            sh, (v, f) = built[r["mesh"]]
+            k = kinds[sh]
+            out.append(dict(w=r["w"], h=r["h"], vp=r["vp"],
+                            draws=[_draw(v, f, k, r["mvp"], 3, tex if k != GOURAUD else None)]))
+        return out
+    raise ValueError(name)
+
+
+def describe(name):
+    return {
+        "cube": {"workload": "textured_cube_640x480", "triangles": 12, "scenes": 1,
+                 "shader": "textured (repeat-pot 64x64 checker)"},
+        "cubes": {"workload": "instanced_cubes_1080p_10k", "triangles": 120_000, "draws": 10_000,
+                  "scenes": 1, "shader": "tex x gouraud (1024x1024 noise)"},
+        "batch": {"workload": "uneven_batch_256", "scenes": 256,
+                  "sizes": "W 64..1920, H 64..1080, 12..200k triangles, log-uniform",
+                  "recipes": "fill-stress or instanced cubes by coin flip"},
+        "serve": {"workload": "serving_poisson", "scenes": 60},
+    }[name]
+
+
+def cpu_sample_indices(name, workers=1):
+    """Scenes the oracle renders for the CPU baseline (about 5-30 s of one
+    core; one share per worker)."""
+    n = len(scenes_for(name))
+    if name == "cube":
+        return [0] * (2000 * workers)
+    if name == "cubes":
+        return [0] * workers
+    if name == "batch":
+        return list(range(n))
+    return list(range(n)) * max(1, workers // 4)
+
+
+def upload(scs, dev):
+    meshes, texes, targets, out = {}, {}, [], []
+    for sc in scs:
+        tg = Framebuf(sc["w"], sc["h"], device=dev)
+        tg.clear()
+        targets.append(tg)
+        items = []
+        for d in sc["draws"]:
+            key = (id(d["verts"]), id(d["faces"]), d["pos_dim"])
+            if key not in meshes:
+                meshes[key] = (Mesh(d["verts"], d["faces"], pos_dim=d["pos_dim"], device=dev),
+                               d["verts"], d["faces"])
+            tex = None
+            if d["tex"] is not None:
+                if id(d["tex"]) not in texes:
+                    texes[id(d["tex"])] = Texture(d["tex"], device=dev)
+                tex = texes[id(d["tex"])]
+            items.append((meshes[key][0], Shader(d["shader"], texture=tex), d["mvp"]))
+        out.append(Scene(tg, items, sc["vp"]))
+    return {"scenes": out, "targets": targets, "meshes": meshes, "textures": texes}
+
+
+def e2e(objs, dev, steps, warmup):
+    """Per step from host buffers (pinned): every mesh's vertices and
+    indices uploaded, every target cleared, the batch rendered, every
+    target's colour + depth read back.  Returns seconds over `steps`, the
+    bytes each way per step and the per-step latency percentiles."""
+    import torch
+    from . import render_batch
+    pins = []
+    h2d = 0
+    for m, v, f in objs["meshes"].values():
+        pv = torch.from_numpy(np.ascontiguousarray(v, np.float32)).pin_memory()
+        pf = torch.from_numpy(np.ascontiguousarray(f, np.uint32).view(np.int32)).pin_memory()
+        pins.append((m, pv.numpy(), pf.numpy().view(np.uint32)))
+        h2d += pv.numel() * 4 + pf.numel() * 4
+    outs = []
+    d2h = 0
+    for tg in objs["targets"]:
+        c = torch.empty((tg.h, tg.w), dtype=torch.int32).pin_memory()
+        d = torch.empty((tg.h, tg.w), dtype=torch.float32).pin_memory()
+        outs.append((tg, c.numpy().view(np.uint32), d.numpy()))
+        d2h += 8 * tg.w * tg.h
+    from . import _fp, _u32p, lib
+
+    def step():
+        for m, v, f in pins:
+            m.update(v, f)
+        for tg in objs["targets"]:
+            tg.clear()
+        render_batch(objs["scenes"], device=dev, sync_stats=False)
+        for tg, c, d in outs:
+            code = lib().rf_target_read(dev.ptr, tg.handle, _u32p(c), _fp(d))
+            if code:
+                raise RuntimeError("rf_target_read: %d" % code)
+
+    for _ in range(warmup):
+        step()
+    lat = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        step()
+        lat.append(time.perf_counter() - t0)
+    ms = sorted(x * 1e3 for x in lat)
+    return {"seconds": sum(lat), "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "latency_ms": {"p50": ms[len(ms) // 2], "p99": ms[min(len(ms) - 1, int(0.99 * len(ms)))]}}
+
+
+def close(objs):
+    for m, _, _ in objs["meshes"].values():
+        m.close()
+    for t in objs["textures"].values():
+        t.close()
+    for tg in objs["targets"]:
+        tg.close()
