@@ -769,14 +769,28 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                             const uint32_t kb = w0 ? (o.px0 / tile_w + 1) * tile_w - o.px0 : 0u;
                             const bool crosses = w0 && o.px0 + kb < o.px1;
                             const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
-                            for (uint32_t c = 0; c < nc; ++c) {
-                                const float cv = T[i][RF_R_C + c], dv = H->dvdx[c];
-                                const float v0 = fadd(cv, fmul(fsub(fadd(cv, dv), cv), tshift));
-                                rec[1 + c] = f2u(v0);
-                                float vb = v0;
-                                for (uint32_t k = 0; k < ksteps; ++k) vb = fadd(vb, dv);  // Iter::next
-                                rec[1 + nc + c] = f2u(vb);
+                            // The components step side by side (independent
+                            // chains), each exactly like Iter::next.
+                            float vb[RF_NC], dvc[RF_NC];
+#pragma unroll
+                            for (uint32_t c = 0; c < RF_NC; ++c) {
+                                if (c < nc) {
+                                    const float cv = T[i][RF_R_C + c];
+                                    dvc[c] = H->dvdx[c];
+                                    vb[c] = fadd(cv, fmul(fsub(fadd(cv, dvc[c]), cv), tshift));
+                                    rec[1 + c] = f2u(vb[c]);
+                                } else {
+                                    dvc[c] = 0.0f;
+                                    vb[c] = 0.0f;
+                                }
                             }
+                            for (uint32_t k = 0; k < ksteps; ++k) {
+#pragma unroll
+                                for (uint32_t c = 0; c < RF_NC; ++c) vb[c] = fadd(vb[c], dvc[c]);
+                            }
+#pragma unroll
+                            for (uint32_t c = 0; c < RF_NC; ++c)
+                                if (c < nc) rec[1 + nc + c] = f2u(vb[c]);
                         }
                         acc_fi += o.frags_i;
                         acc_oob += o.oob;

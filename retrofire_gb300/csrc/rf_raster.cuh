@@ -85,9 +85,16 @@ struct Kind {
     }
 };
 
+// Depth bounds of the FAST path: per lane, the minimum current depth of each
+// RF_SEG-pixel segment of its tile row (shared memory, word s*32 + lane).
+// Under the Less test with depth writes a pixel's depth only grows, so a
+// stored minimum stays a lower bound until it is refreshed.
+#define RF_SEG 8
+
 struct TileCtx {
     uint32_t *scol;
     float *sdep;
+    float *smin;
     uint32_t lane;
     uint32_t y;       // this lane's row
     uint32_t tx0;     // first column of the tile
@@ -104,8 +111,8 @@ struct TileCtx {
 // Fragments a..b-1 of one scanline into the tile (raster.rs:60-69,
 // target.rs:163-198): v = varyings of fragment a, stepped by dv per pixel.
 template <int KIND, bool FAST>
-__device__ __forceinline__ void pixels(TileCtx &T, const DrawDev &d, float *v, const float *dv,
-                                       uint32_t a, uint32_t b) {
+__device__ __forceinline__ uint32_t pixels(TileCtx &T, const DrawDev &d, float *v, const float *dv,
+                                           uint32_t a, uint32_t b) {
     constexpr int NC = Kind<KIND>::NC;
     uint32_t idx = (a - T.tx0) * RF_TILE_H + T.lane;
     const uint32_t end = (b - T.tx0) * RF_TILE_H + T.lane;
@@ -158,6 +165,7 @@ __device__ __forceinline__ void pixels(TileCtx &T, const DrawDev &d, float *v, c
             for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
         }
         T.frags_o += nout;
+        return nout;
     } else {
         for (; idx != end; idx += RF_TILE_H) {
             const float z = v[0];
@@ -181,7 +189,41 @@ __device__ __forceinline__ void pixels(TileCtx &T, const DrawDev &d, float *v, c
     #pragma unroll
             for (int c = 0; c < NC; ++c) v[c] = fadd(v[c], dv[c]);
         }
+        return 0;
     }
+}
+
+// FAST path: the minimum current depth of segment s of the lane's row.
+__device__ __forceinline__ void seg_refresh(TileCtx &T, uint32_t s) {
+    const uint32_t base = s * RF_SEG * RF_TILE_H + T.lane;
+    float m = T.sdep[base];
+#pragma unroll
+    for (uint32_t x = 1; x < RF_SEG; ++x) m = fminf(m, T.sdep[base + x * RF_TILE_H]);
+    T.smin[s * RF_TILE_H + T.lane] = m;
+}
+
+// FAST path: true when no fragment a..b-1 can pass Less: an upper bound of
+// the span's running z is <= the current depth of every pixel it covers.
+// z_k = fl(z_{k-1} + dz) never rises when dz <= 0, so its maximum is za; for
+// dz > 0 (all values positive, normal range) k <= 63 rounded additions stay
+// within (1+2^-24)^k of za + k dz, and fl(za + k dz) is within (1-2^-24)^2
+// of it, so fl(e * (1 + 2^-16)) bounds every z_k.  NaN z or depth never
+// skips here (the comparisons are false) and never passes later.
+__device__ __forceinline__ bool span_hidden(const TileCtx &T, float za, float dz, uint32_t a,
+                                            uint32_t b) {
+    float zhi;
+    if (dz <= 0.0f) {
+        zhi = za;
+    } else if (dz > 0.0f && za >= 1e-30f) {
+        const float e = fadd(za, fmul((float)(b - a - 1u), dz));
+        zhi = fmul(e, 1.0000152587890625f);  // 1 + 2^-16
+    } else {
+        return false;
+    }
+    const uint32_t s0 = (a - T.tx0) / RF_SEG, s1 = (b - 1u - T.tx0) / RF_SEG;
+    float lo = T.smin[s0 * RF_TILE_H + T.lane];
+    for (uint32_t s = s0 + 1; s <= s1; ++s) lo = fminf(lo, T.smin[s * RF_TILE_H + T.lane]);
+    return zhi <= lo;
 }
 
 // The lane's scanline j of half H (raster.rs:84-113), clipped to the tile,
@@ -272,87 +314,92 @@ __device__ __forceinline__ void raster_prim_k(TileCtx &T, const DrawDev &d, cons
     }
 }
 
-// A triangle with row records: the lane's row record, loaded into
-// registers one triangle ahead of its use (the loads overlap the previous
-// triangle's pixels).
-template <int NC>
-struct RowPreT {
-    uint32_t w0;  // first pixel | end << 16; 0 when the row has no record
-    uint32_t hh;  // half of the scanline
-    float v[NC];  // varyings at the span's first pixel
-    float vb[NC]; // ... and at its first tile boundary
-};
-// Components held for a kernel: its kind's, or all for RF_K_ANY.
+// Row records in shared memory: per staged triangle one slot of
+// RF_ROW_WORDS(NC) words per lane, word w of lane L at w * 32 + L (the bank
+// is the lane).  Each lane copies its own row's record (cp.async, 4 bytes a
+// word) two triangles ahead of its use; a lane whose row the triangle does
+// not cover stores word 0 = 0 (an empty span).
 template <int KIND>
 struct PreNC {
     static constexpr int NC = KIND == RF_K_ANY ? RF_NC : Kind<KIND == RF_K_ANY ? 0 : KIND>::NC;
 };
-template <int KIND>
-using RowPre = RowPreT<PreNC<KIND>::NC>;
+__host__ __device__ constexpr uint32_t row_words(int nc) { return 1u + 2u * (uint32_t)nc; }
 
 template <int KIND>
-__device__ __forceinline__ RowPre<KIND> row_prefetch(const TileCtx &T, const RasterPrim *__restrict__ R,
-                                                     const uint32_t *__restrict__ rows) {
-    RowPre<KIND> q;
-    q.w0 = 0;
-    q.hh = 0;
-    if (!T.row_ok || (R->flags & (RF_RP_LIVE | RF_RP_ROWS)) != (RF_RP_LIVE | RF_RP_ROWS)) return q;
+__device__ __forceinline__ void stage_rows(const TileCtx &T, uint32_t *slot, const RasterPrim *R,
+                                           const uint32_t *__restrict__ rows) {
+    uint32_t *dst = slot + T.lane;
+    if (!R || !T.row_ok || (R->flags & (RF_RP_LIVE | RF_RP_ROWS)) != (RF_RP_LIVE | RF_RP_ROWS)) {
+        dst[0] = 0u;
+        return;
+    }
     const uint32_t y = T.y;
     uint32_t j;
     if (y - R->y0 < R->c0) {
         j = y - R->y0;
     } else if (y - R->y1 < R->c1) {
         j = R->c0 + (y - R->y1);
-        q.hh = 1;
     } else {
-        return q;
+        dst[0] = 0u;
+        return;
     }
-    const uint32_t *rec = rows + R->base + (size_t)j * R->stride;
-    q.w0 = __ldg(rec);
-    if (KIND != RF_K_ANY) {
-        constexpr int NC = PreNC<KIND>::NC;
+    const uint32_t stride = R->stride;  // 1 + 2 NC of the triangle's own kind
+    const uint32_t *src = rows + R->base + (size_t)j * stride;
+    const uint32_t nw = KIND == RF_K_ANY ? stride : row_words(PreNC<KIND>::NC);
 #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            q.v[c] = u2f(__ldg(rec + 1 + c));
-            q.vb[c] = u2f(__ldg(rec + 1 + NC + c));
-        }
-    } else {
-        const uint32_t nc = (R->stride - 1) / 2;
-#pragma unroll
-        for (int c = 0; c < PreNC<KIND>::NC; ++c) {
-            q.v[c] = (uint32_t)c < nc ? u2f(__ldg(rec + 1 + c)) : 0.0f;
-            q.vb[c] = (uint32_t)c < nc ? u2f(__ldg(rec + 1 + nc + c)) : 0.0f;
+    for (uint32_t w = 0; w < row_words(PreNC<KIND>::NC); ++w) {
+        if (w < nw) {
+            const uint32_t sa = (uint32_t)__cvta_generic_to_shared(dst + w * RF_TILE_H);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src + w) : "memory");
         }
     }
-    return q;
 }
 
-template <int KIND, bool FAST, int QN>
+template <int KIND, bool FAST>
 __device__ __forceinline__ void raster_rows(TileCtx &T, const DrawDev &d, const RasterPrim *__restrict__ R,
-                                            const RowPreT<QN> &q) {
-    static_assert(QN >= Kind<KIND>::NC, "prefetched record too short");
+                                            uint32_t *slot) {
     constexpr int NC = Kind<KIND>::NC;
-    const uint32_t xs = q.w0 & 0xFFFFu, xe = q.w0 >> 16;
+    uint32_t *rs = slot + T.lane;
+    const uint32_t w0 = rs[0];
+    const uint32_t xs = w0 & 0xFFFFu, xe = w0 >> 16;
     const uint32_t a = xs > T.tx0 ? xs : T.tx0;
     const uint32_t b = xe < T.tx1 ? xe : T.tx1;
     if (a >= b) return;
+    const uint32_t hh = T.y - R->y0 < R->c0 ? 0u : 1u;
     // The span starts in this tile (k = 0 from its first pixel) or enters it
     // at a tile boundary at or after its first one (k steps from there).
     const bool first = a == xs;
     const uint32_t k = first ? 0u : a - ((xs & ~(T.tw - 1u)) + T.tw);
+    const uint32_t off = first ? 1u : 1u + NC;
+    if (k) {
+        // A third or later tile of the span: step the boundary values in
+        // place (the lane's own slot), one component at a time (a rolled
+        // loop keeps the jump's code out of the per-component unrolling).
+#pragma unroll 1
+        for (int c = 0; c < NC; ++c)
+            rs[(off + c) * RF_TILE_H] = f2u(jump(u2f(rs[(off + c) * RF_TILE_H]), R->dvdx[hh][c], k));
+    }
     float v[NC], dv[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-        dv[c] = R->dvdx[q.hh][c];
-        v[c] = jump(first ? q.v[c] : q.vb[c], dv[c], k);
+        dv[c] = R->dvdx[hh][c];
+        v[c] = u2f(rs[(off + c) * RF_TILE_H]);
     }
-    pixels<KIND, FAST>(T, d, v, dv, a, b);
+    if constexpr (FAST) {
+        if (span_hidden(T, v[0], dv[0], a, b)) return;
+        if (pixels<KIND, FAST>(T, d, v, dv, a, b)) {
+            const uint32_t s1 = (b - 1u - T.tx0) / RF_SEG;
+            for (uint32_t s = (a - T.tx0) / RF_SEG; s <= s1; ++s) seg_refresh(T, s);
+        }
+    } else {
+        pixels<KIND, FAST>(T, d, v, dv, a, b);
+    }
 }
 
-template <int KIND, bool FAST, int QN>
+template <int KIND, bool FAST>
 __device__ __forceinline__ void raster_one(TileCtx &T, const DrawDev &d, const RasterPrim *__restrict__ R,
-                                           const PrimRec *__restrict__ P, const RowPreT<QN> &q) {
-    if (R->flags & RF_RP_ROWS) raster_rows<KIND, FAST, QN>(T, d, R, q);
+                                           const PrimRec *__restrict__ P, uint32_t *rs) {
+    if (R->flags & RF_RP_ROWS) raster_rows<KIND, FAST>(T, d, R, rs);
     else raster_prim_k<KIND, FAST>(T, d, P);
 }
 
@@ -361,35 +408,35 @@ __device__ __forceinline__ void raster_one(TileCtx &T, const DrawDev &d, const R
 template <int KIND, bool FAST>
 __device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restrict__ draws,
                                             const RasterPrim *__restrict__ R,
-                                            const PrimRec *__restrict__ P, const RowPre<KIND> &q) {
+                                            const PrimRec *__restrict__ P, uint32_t *rs) {
     if (!(R->flags & RF_RP_LIVE)) return;
     const DrawDev &d = draws[R->draw];
     if constexpr (KIND != RF_K_ANY) {
-        raster_one<KIND == RF_K_ANY ? 0 : KIND, FAST, PreNC<KIND>::NC>(T, d, R, P, q);
+        raster_one<KIND == RF_K_ANY ? 0 : KIND, FAST>(T, d, R, P, rs);
     } else {
-    switch (R->kind) {
-        case RF_K_FLAT: raster_one<RF_K_FLAT, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
-        case RF_K_GOURAUD: raster_one<RF_K_GOURAUD, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
-        case RF_K_TEXTURED: raster_one<RF_K_TEXTURED, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
-        case RF_K_TEX_GOURAUD: raster_one<RF_K_TEX_GOURAUD, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
-        default: raster_one<RF_K_GOURAUD_SRGB, FAST, PreNC<KIND>::NC>(T, d, R, P, q); break;
-    }
+        switch (R->kind) {
+            case RF_K_FLAT: raster_one<RF_K_FLAT, FAST>(T, d, R, P, rs); break;
+            case RF_K_GOURAUD: raster_one<RF_K_GOURAUD, FAST>(T, d, R, P, rs); break;
+            case RF_K_TEXTURED: raster_one<RF_K_TEXTURED, FAST>(T, d, R, P, rs); break;
+            case RF_K_TEX_GOURAUD: raster_one<RF_K_TEX_GOURAUD, FAST>(T, d, R, P, rs); break;
+            default: raster_one<RF_K_GOURAUD_SRGB, FAST>(T, d, R, P, rs); break;
+        }
     }
 }
 
 // Walks a tile's bitmask in submission order: set bits of the mask words
 // (input triangles), each expanded to its clipped output triangles.  The
-// offsets of the next input triangle are loaded one triangle ahead, so
-// their latency overlaps the current triangle.  Warp-uniform state; every
-// lane calls next() together.
+// next 32 input triangles are gathered at once, lane k holding the k-th
+// one's output range (toff, tcnt loaded in parallel), so one load latency
+// covers 32 triangles.  Warp-uniform state; every lane calls next() together.
 struct PrimIter {
     const uint32_t *tmask;
     const uint32_t *toff;
     const uint32_t *tcnt;
     uint32_t nwords, tri_base, lane;
     uint32_t wb, word, bal, src, wv, p, pend;
-    uint32_t la_off, la_cnt;  // loads in flight for the look-ahead triangle
-    bool started, has_la;
+    uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
+    bool started;
     // Next set bit (input triangle, global index) or false.
     __device__ __forceinline__ bool next_bit(uint32_t &gt) {
         for (;;) {
@@ -412,32 +459,40 @@ struct PrimIter {
             bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
         }
     }
-    __device__ __forceinline__ void look_ahead() {
-        uint32_t gt;
-        has_la = next_bit(gt);
-        if (has_la) {
-            la_off = __ldg(toff + gt);
-            la_cnt = __ldg(tcnt + gt);
+    __device__ __forceinline__ void refill() {
+        uint32_t mine = 0, n = 0, gt;
+        while (n < 32u && next_bit(gt)) {
+            if (lane == n) mine = gt;
+            ++n;
+        }
+        bn = n;
+        bi = 0;
+        if (lane < n) {
+            boff = __ldg(toff + mine);
+            bcnt = __ldg(tcnt + mine);
         }
     }
     __device__ __forceinline__ void init() {
         wb = word = bal = src = wv = p = pend = 0;
+        boff = bcnt = bn = bi = 0;
         started = false;
-        look_ahead();
     }
     __device__ __forceinline__ uint32_t next() {
         while (p >= pend) {
-            if (!has_la) return 0xFFFFFFFFu;
-            p = la_off;
-            pend = la_off + la_cnt;
-            look_ahead();
+            if (bi >= bn) {
+                refill();
+                if (bn == 0) return 0xFFFFFFFFu;
+            }
+            p = __shfl_sync(0xFFFFFFFFu, boff, bi);
+            pend = p + __shfl_sync(0xFFFFFFFFu, bcnt, bi);
+            ++bi;
         }
         return p++;
     }
 };
 
 // Asynchronous copy of one triangle header into this warp's staging slot
-// (16 bytes per lane; one commit group per call on every lane).
+// (16 bytes per lane, lanes 0..5); committed by commit_stage().
 __device__ __forceinline__ void stage_prim(RasterPrim *slot, const RasterPrim *src, uint32_t lane) {
     static_assert(sizeof(RasterPrim) % 16 == 0, "RasterPrim must be a whole number of 16-byte chunks");
     static_assert(sizeof(RasterPrim) <= 64 * 16, "RasterPrim is staged in at most two rounds");
@@ -451,9 +506,13 @@ __device__ __forceinline__ void stage_prim(RasterPrim *slot, const RasterPrim *s
                          : "memory");
         }
     }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
+// One commit group per call on every lane (copies issued since the last).
+__device__ __forceinline__ void commit_stage() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+// All but the N most recent groups of this lane complete, and visible to
+// the whole warp.
 template <int N>
 __device__ __forceinline__ void wait_staged_but() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
@@ -461,6 +520,18 @@ __device__ __forceinline__ void wait_staged_but() {
 }
 
 }  // namespace rfr
+
+// Shared-memory words per warp: colour and depth tiles, three staged
+// triangle headers, the depth-segment minima.
+// Header ring: triangles i .. i+4 (RF_HDR_SLOTS); row-record ring:
+// triangles i .. i+2 (RF_ROW_SLOTS).
+#define RF_HDR_SLOTS 5u
+#define RF_ROW_SLOTS 3u
+template <int TW, int KIND>
+__host__ __device__ constexpr uint32_t raster_warp_words() {
+    return 2u * TW * RF_TILE_H + RF_HDR_SLOTS * (uint32_t)(sizeof(RasterPrim) / 4) +
+           RF_ROW_SLOTS * rfr::row_words(rfr::PreNC<KIND>::NC) * RF_TILE_H + ((uint32_t)TW / RF_SEG) * RF_TILE_H;
+}
 
 // KIND: shader kind of every draw of the job (or RF_K_ANY); FAST: the
 // default context (depth test Less, colour and depth writes) on a target
@@ -475,10 +546,13 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
     using namespace rfr;
     extern __shared__ __align__(16) uint32_t smem[];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr uint32_t WARP_WORDS = 2 * TW * RF_TILE_H + 3 * (sizeof(RasterPrim) / 4);
+    constexpr uint32_t WARP_WORDS = raster_warp_words<TW, KIND>();
+    constexpr uint32_t RW = row_words(PreNC<KIND>::NC) * RF_TILE_H;  // words per row slot
     uint32_t *scol = smem + warp * WARP_WORDS;
     float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
     RasterPrim *stage = reinterpret_cast<RasterPrim *>(scol + 2 * TW * RF_TILE_H);
+    uint32_t *rslots = scol + 2 * TW * RF_TILE_H + RF_HDR_SLOTS * (sizeof(RasterPrim) / 4);
+    float *smin = reinterpret_cast<float *>(rslots + RF_ROW_SLOTS * RW);
     for (;;) {
         uint32_t tile = 0;
         if (lane == 0) tile = atomicAdd(tile_queue, 1u);
@@ -491,6 +565,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         TileCtx T;
         T.scol = scol;
         T.sdep = sdep;
+        T.smin = smin;
         T.lane = lane;
         T.tx0 = txi * TW;
         T.tx1 = min(T.tx0 + (uint32_t)TW, J.w);
@@ -537,6 +612,12 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
                 }
             }
         };
+        auto load_tile_and_bounds = [&]() {
+            load_tile();
+            if constexpr (FAST) {
+                for (uint32_t sg = 0; sg < (uint32_t)TW / RF_SEG; ++sg) seg_refresh(T, sg);
+            }
+        };
         PrimIter it;
         it.tmask = mask + J.mask_base + (size_t)lt * J.mask_words;
         it.toff = toff;
@@ -545,45 +626,55 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         it.tri_base = J.tri_base;
         it.lane = lane;
         it.init();
-        // Double-buffered: the record of the next triangle is in flight
-        // while the current one is rasterised.
-        // Three staging slots: triangle i is rasterised while the header of
-        // i+2 is in flight and the row records of i+1 load into registers.
-        // Prims p0 (current), p1, p2 in slots s0, s1, s2; the slots rotate.
+        // Software pipeline over the tile's triangles t0, t1, ...: iteration
+        // i rasterises t_i while the row records of t_{i+2} and the header
+        // of t_{i+4} are in flight (one cp.async group per iteration, G_i).
+        // Waiting for all but the newest group at the top of iteration i
+        // completes G_{i-2}: the header of t_{i+2} (needed for its row
+        // address) and the row records of t_i.
         constexpr uint32_t NONE = 0xFFFFFFFFu;
         uint32_t p0 = it.next();
         if (p0 != NONE) {
-            load_tile();
+            load_tile_and_bounds();
             loaded = true;
+            const uint32_t p1 = it.next();
+            const uint32_t p2 = p1 != NONE ? it.next() : NONE;
+            const uint32_t p3 = p2 != NONE ? it.next() : NONE;
             stage_prim(stage + 0, rprims + p0, lane);
-            uint32_t p1 = it.next();
+            commit_stage();
             stage_prim(stage + 1, p1 != NONE ? rprims + p1 : nullptr, lane);
-            uint32_t p2 = p1 != NONE ? it.next() : NONE;
+            commit_stage();
+            wait_staged_but<1>();
             stage_prim(stage + 2, p2 != NONE ? rprims + p2 : nullptr, lane);
-            wait_staged_but<2>();
-            RowPre<KIND> q = row_prefetch<KIND>(T, stage + 0, rows);
-            uint32_t s0 = 0, s1 = 1, s2 = 2;
+            stage_rows<KIND>(T, rslots + 0 * RW, stage + 0, rows);
+            commit_stage();
+            wait_staged_but<1>();
+            stage_prim(stage + 3, p3 != NONE ? rprims + p3 : nullptr, lane);
+            stage_rows<KIND>(T, rslots + 1 * RW, p1 != NONE ? stage + 1 : nullptr, rows);
+            commit_stage();
+            uint32_t q0 = p0, q1 = p1, q2 = p2, q3 = p3;
+            uint32_t h = 0, r = 0;  // slots of t_i: header h (mod 5), rows r (mod 3)
             for (;;) {
                 wait_staged_but<1>();
-                RowPre<KIND> qn;
-                qn.w0 = 0;
-                qn.hh = 0;
-                if (p1 != NONE) qn = row_prefetch<KIND>(T, stage + s1, rows);
-                raster_prim<KIND, FAST>(T, draws, stage + s0, prims + p0, q);
+                const uint32_t q4 = q3 != NONE ? it.next() : NONE;
+                const uint32_t h2 = h + 2 >= RF_HDR_SLOTS ? h + 2 - RF_HDR_SLOTS : h + 2;
+                const uint32_t h4 = h + 4 >= RF_HDR_SLOTS ? h + 4 - RF_HDR_SLOTS : h + 4;
+                const uint32_t r2 = r + 2 >= RF_ROW_SLOTS ? r + 2 - RF_ROW_SLOTS : r + 2;
+                stage_rows<KIND>(T, rslots + r2 * RW, q2 != NONE ? stage + h2 : nullptr, rows);
+                stage_prim(stage + h4, q4 != NONE ? rprims + q4 : nullptr, lane);
+                commit_stage();
+                raster_prim<KIND, FAST>(T, draws, stage + h, prims + q0, rslots + r * RW);
                 __syncwarp();
-                if (p1 == NONE) break;
-                const uint32_t p3 = p2 != NONE ? it.next() : NONE;
-                stage_prim(stage + s0, p3 != NONE ? rprims + p3 : nullptr, lane);
-                q = qn;
-                p0 = p1;
-                p1 = p2;
-                p2 = p3;
-                const uint32_t t = s0;
-                s0 = s1;
-                s1 = s2;
-                s2 = t;
+                if (q1 == NONE) break;
+                q0 = q1;
+                q1 = q2;
+                q2 = q3;
+                q3 = q4;
+                h = h + 1 == RF_HDR_SLOTS ? 0 : h + 1;
+                r = r + 1 == RF_ROW_SLOTS ? 0 : r + 1;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
+            __syncwarp();
         }
         if (!loaded && J.clear_flags) {
             load_tile();
@@ -623,7 +714,7 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
                                    const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
                                    uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
                                    cudaStream_t s) {
-    const size_t smem = (size_t)warps * (2 * TW * RF_TILE_H * 4 + 3 * sizeof(RasterPrim));
+    const size_t smem = (size_t)warps * raster_warp_words<TW, KIND>() * 4;
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_raster<TW, KIND, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
