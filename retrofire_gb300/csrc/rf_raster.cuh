@@ -325,26 +325,50 @@ struct PreNC {
 };
 __host__ __device__ constexpr uint32_t row_words(int nc) { return 1u + 2u * (uint32_t)nc; }
 
+// Word indices of RasterPrim fields (the header travels as 24 words, word k
+// in lane k, while it is in flight).
+#define RF_RPW_FLAGS 1
+#define RF_RPW_BASE 3
+#define RF_RPW_STRIDE 4
+#define RF_RPW_Y0 5
+#define RF_RPW_C0 6
+#define RF_RPW_Y1 7
+#define RF_RPW_C1 8
+static_assert(offsetof(RasterPrim, flags) == 4 * RF_RPW_FLAGS && offsetof(RasterPrim, base) == 4 * RF_RPW_BASE &&
+                  offsetof(RasterPrim, stride) == 4 * RF_RPW_STRIDE && offsetof(RasterPrim, y0) == 4 * RF_RPW_Y0 &&
+                  offsetof(RasterPrim, c0) == 4 * RF_RPW_C0 && offsetof(RasterPrim, y1) == 4 * RF_RPW_Y1 &&
+                  offsetof(RasterPrim, c1) == 4 * RF_RPW_C1,
+              "RasterPrim word layout");
+
+// Row records of one triangle whose header is spread over the warp (word k
+// of the header in lane k's hw); present = the triangle exists.  Every lane
+// calls this together (the fields are shuffled out of hw).
 template <int KIND>
-__device__ __forceinline__ void stage_rows(const TileCtx &T, uint32_t *slot, const RasterPrim *R,
+__device__ __forceinline__ void stage_rows(const TileCtx &T, uint32_t *slot, bool present, uint32_t hw,
                                            const uint32_t *__restrict__ rows) {
+    const uint32_t flags = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_FLAGS);
+    const uint32_t rbase = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_BASE);
+    const uint32_t stride = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_STRIDE);  // 1 + 2 NC of its own kind
+    const uint32_t y0 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_Y0);
+    const uint32_t c0 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_C0);
+    const uint32_t y1 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_Y1);
+    const uint32_t c1 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_C1);
     uint32_t *dst = slot + T.lane;
-    if (!R || !T.row_ok || (R->flags & (RF_RP_LIVE | RF_RP_ROWS)) != (RF_RP_LIVE | RF_RP_ROWS)) {
+    if (!present || !T.row_ok || (flags & (RF_RP_LIVE | RF_RP_ROWS)) != (RF_RP_LIVE | RF_RP_ROWS)) {
         dst[0] = 0u;
         return;
     }
     const uint32_t y = T.y;
     uint32_t j;
-    if (y - R->y0 < R->c0) {
-        j = y - R->y0;
-    } else if (y - R->y1 < R->c1) {
-        j = R->c0 + (y - R->y1);
+    if (y - y0 < c0) {
+        j = y - y0;
+    } else if (y - y1 < c1) {
+        j = c0 + (y - y1);
     } else {
         dst[0] = 0u;
         return;
     }
-    const uint32_t stride = R->stride;  // 1 + 2 NC of the triangle's own kind
-    const uint32_t *src = rows + R->base + (size_t)j * stride;
+    const uint32_t *src = rows + rbase + (size_t)j * stride;
     const uint32_t nw = KIND == RF_K_ANY ? stride : row_words(PreNC<KIND>::NC);
 #pragma unroll
     for (uint32_t w = 0; w < row_words(PreNC<KIND>::NC); ++w) {
@@ -434,7 +458,9 @@ struct PrimIter {
     const uint32_t *toff;
     const uint32_t *tcnt;
     uint32_t nwords, tri_base, lane;
-    uint32_t wb, word, bal, src, wv, p, pend;
+    // Mask words are read 128 at a time (lane L holds words wb + 32 c + L,
+    // c = 0..3) so one load round covers four ballots.
+    uint32_t wb, w1, w2, w3, word, chunk, bal, src, wv, p, pend;
     uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
     bool started;
     // Next set bit (input triangle, global index) or false.
@@ -443,7 +469,7 @@ struct PrimIter {
             if (wv) {
                 const uint32_t b = __ffs(wv) - 1;
                 wv &= wv - 1;
-                gt = tri_base + (wb + src) * 32 + b;
+                gt = tri_base + (wb + chunk * 32 + src) * 32 + b;
                 return true;
             }
             if (bal) {
@@ -452,10 +478,21 @@ struct PrimIter {
                 wv = __shfl_sync(0xFFFFFFFFu, word, src);
                 continue;
             }
-            if (started) wb += 32;
+            if (started && chunk < 3) {
+                ++chunk;
+                word = chunk == 1 ? w1 : (chunk == 2 ? w2 : w3);
+                bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
+                continue;
+            }
+            if (started) wb += 128;
             started = true;
             if (wb >= nwords) return false;
-            word = wb + lane < nwords ? tmask[wb + lane] : 0u;
+            const uint32_t i0 = wb + lane;
+            word = i0 < nwords ? tmask[i0] : 0u;
+            w1 = i0 + 32 < nwords ? tmask[i0 + 32] : 0u;
+            w2 = i0 + 64 < nwords ? tmask[i0 + 64] : 0u;
+            w3 = i0 + 96 < nwords ? tmask[i0 + 96] : 0u;
+            chunk = 0;
             bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
         }
     }
@@ -473,7 +510,7 @@ struct PrimIter {
         }
     }
     __device__ __forceinline__ void init() {
-        wb = word = bal = src = wv = p = pend = 0;
+        wb = w1 = w2 = w3 = word = chunk = bal = src = wv = p = pend = 0;
         boff = bcnt = bn = bi = 0;
         started = false;
     }
@@ -523,10 +560,14 @@ __device__ __forceinline__ void wait_staged_but() {
 
 // Shared-memory words per warp: colour and depth tiles, three staged
 // triangle headers, the depth-segment minima.
-// Header ring: triangles i .. i+4 (RF_HDR_SLOTS); row-record ring:
-// triangles i .. i+2 (RF_ROW_SLOTS).
-#define RF_HDR_SLOTS 5u
-#define RF_ROW_SLOTS 3u
+// Pipeline distances of the rasteriser: a triangle's header is loaded into
+// registers RF_HDR_AHEAD triangles before its turn, its row records are
+// copied into shared memory RF_ROW_AHEAD before (a ring of RF_ROW_SLOTS);
+// the header of the current triangle sits in one shared-memory slot.
+#define RF_HDR_AHEAD 8
+#define RF_ROW_AHEAD 2
+#define RF_HDR_SLOTS 1u
+#define RF_ROW_SLOTS (RF_ROW_AHEAD + 1u)
 template <int TW, int KIND>
 __host__ __device__ constexpr uint32_t raster_warp_words() {
     return 2u * TW * RF_TILE_H + RF_HDR_SLOTS * (uint32_t)(sizeof(RasterPrim) / 4) +
@@ -627,50 +668,54 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         it.lane = lane;
         it.init();
         // Software pipeline over the tile's triangles t0, t1, ...: iteration
-        // i rasterises t_i while the row records of t_{i+2} and the header
-        // of t_{i+4} are in flight (one cp.async group per iteration, G_i).
-        // Waiting for all but the newest group at the top of iteration i
-        // completes G_{i-2}: the header of t_{i+2} (needed for its row
-        // address) and the row records of t_i.
+        // i rasterises t_i while the headers of t_{i+1} .. t_{i+HA} are in
+        // flight or held in registers (hw[k]: word `lane` of t_{i+k}'s
+        // header; ordinary loads, so a register waits only when it is used)
+        // and the row records of t_{i+1} .. t_{i+RA} are in flight as
+        // cp.async groups, one per triangle in order.  Iteration i commits
+        // the group of t_{i+RA}; the rows of t_i are then complete once all
+        // but the newest RA groups are.
         constexpr uint32_t NONE = 0xFFFFFFFFu;
-        uint32_t p0 = it.next();
-        if (p0 != NONE) {
+        constexpr int HA = RF_HDR_AHEAD, RA = RF_ROW_AHEAD;
+        constexpr uint32_t HWN = sizeof(RasterPrim) / 4;
+        static_assert(RA >= 1 && HA >= RA && HWN <= 32, "pipeline shape");
+        const uint32_t *rpw = reinterpret_cast<const uint32_t *>(rprims);
+        auto hload = [&](uint32_t t) -> uint32_t {
+            return t != NONE && lane < HWN ? __ldg(rpw + (size_t)t * HWN + lane) : 0u;
+        };
+        uint32_t q[HA + 1];   // t_i .. t_{i+HA}
+        uint32_t hw[HA + 1];  // their header words
+        q[0] = it.next();
+        if (q[0] != NONE) {
             load_tile_and_bounds();
             loaded = true;
-            const uint32_t p1 = it.next();
-            const uint32_t p2 = p1 != NONE ? it.next() : NONE;
-            const uint32_t p3 = p2 != NONE ? it.next() : NONE;
-            stage_prim(stage + 0, rprims + p0, lane);
-            commit_stage();
-            stage_prim(stage + 1, p1 != NONE ? rprims + p1 : nullptr, lane);
-            commit_stage();
-            wait_staged_but<1>();
-            stage_prim(stage + 2, p2 != NONE ? rprims + p2 : nullptr, lane);
-            stage_rows<KIND>(T, rslots + 0 * RW, stage + 0, rows);
-            commit_stage();
-            wait_staged_but<1>();
-            stage_prim(stage + 3, p3 != NONE ? rprims + p3 : nullptr, lane);
-            stage_rows<KIND>(T, rslots + 1 * RW, p1 != NONE ? stage + 1 : nullptr, rows);
-            commit_stage();
-            uint32_t q0 = p0, q1 = p1, q2 = p2, q3 = p3;
-            uint32_t h = 0, r = 0;  // slots of t_i: header h (mod 5), rows r (mod 3)
-            for (;;) {
-                wait_staged_but<1>();
-                const uint32_t q4 = q3 != NONE ? it.next() : NONE;
-                const uint32_t h2 = h + 2 >= RF_HDR_SLOTS ? h + 2 - RF_HDR_SLOTS : h + 2;
-                const uint32_t h4 = h + 4 >= RF_HDR_SLOTS ? h + 4 - RF_HDR_SLOTS : h + 4;
-                const uint32_t r2 = r + 2 >= RF_ROW_SLOTS ? r + 2 - RF_ROW_SLOTS : r + 2;
-                stage_rows<KIND>(T, rslots + r2 * RW, q2 != NONE ? stage + h2 : nullptr, rows);
-                stage_prim(stage + h4, q4 != NONE ? rprims + q4 : nullptr, lane);
+#pragma unroll
+            for (int k = 1; k <= HA; ++k) q[k] = q[k - 1] != NONE ? it.next() : NONE;
+#pragma unroll
+            for (int k = 0; k <= HA; ++k) hw[k] = hload(q[k]);
+#pragma unroll
+            for (int k = 0; k < RA; ++k) {
+                stage_rows<KIND>(T, rslots + k * RW, q[k] != NONE, hw[k], rows);
                 commit_stage();
-                raster_prim<KIND, FAST>(T, draws, stage + h, prims + q0, rslots + r * RW);
+            }
+            uint32_t r = 0;  // row slot of t_i (mod RA+1)
+            for (;;) {
+                const uint32_t rr = r == 0 ? RF_ROW_SLOTS - 1 : r - 1;  // t_{i+RA}: t_{i-1}'s old slot
+                stage_rows<KIND>(T, rslots + rr * RW, q[RA] != NONE, hw[RA], rows);
+                commit_stage();
+                if (lane < HWN) reinterpret_cast<uint32_t *>(stage)[lane] = hw[0];
+                wait_staged_but<RA>();
+                raster_prim<KIND, FAST>(T, draws, stage, prims + q[0], rslots + r * RW);
                 __syncwarp();
-                if (q1 == NONE) break;
-                q0 = q1;
-                q1 = q2;
-                q2 = q3;
-                q3 = q4;
-                h = h + 1 == RF_HDR_SLOTS ? 0 : h + 1;
+                if (q[1] == NONE) break;
+                const uint32_t qn = q[HA] != NONE ? it.next() : NONE;
+#pragma unroll
+                for (int k = 0; k < HA; ++k) {
+                    q[k] = q[k + 1];
+                    hw[k] = hw[k + 1];
+                }
+                q[HA] = qn;
+                hw[HA] = hload(qn);
                 r = r + 1 == RF_ROW_SLOTS ? 0 : r + 1;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
@@ -714,10 +759,15 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
                                    const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
                                    uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
                                    cudaStream_t s) {
-    const size_t smem = (size_t)warps * raster_warp_words<TW, KIND>() * 4;
+    // Shared memory per block: at most the 227 KB opt-in limit, so the
+    // block takes as many warps as fit (wide tiles of the generic kind).
+    constexpr size_t SMEM_MAX = 227 * 1024;
+    constexpr size_t per_warp = (size_t)raster_warp_words<TW, KIND>() * 4;
+    if ((size_t)warps * per_warp > SMEM_MAX) warps = (uint32_t)(SMEM_MAX / per_warp);
+    const size_t smem = (size_t)warps * per_warp;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_raster<TW, KIND, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_raster<TW, KIND, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_MAX);
         attr_set = true;
     }
     int per_sm = 0;
