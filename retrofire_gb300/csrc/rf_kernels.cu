@@ -416,24 +416,28 @@ __device__ void scan_setup(float y0, float y1, const SV &l0, const SV &l1, const
             st[RF_R_C + c] = 0.0f;
         }
     }
-    for (uint32_t r = 0; r < RF_NR; ++r) {
-        // Run 0 from the first row; run 1 after one explicit addition.
-        uint32_t k0, k1;
-        fast_params(st[r], h.d[r], h.i0[r], k0);
-        h.b0[r] = f2u(st[r]);
-        h.e0[r] = k0;
-        if (k0 == 0xFFFFFFFFu) {  // fixed point: run 0 covers every row
-            h.b1[r] = h.b0[r];
-            h.i1[r] = 0;
-            h.e1[r] = k0;
-            continue;
-        }
-        const float v1 = fadd(u2f(h.b0[r] + k0 * (uint32_t)h.i0[r]), h.d[r]);
-        fast_params(v1, h.d[r], h.i1[r], k1);
-        h.b1[r] = f2u(v1);
-        const uint64_t e1 = (uint64_t)k0 + 1u + k1;
-        h.e1[r] = e1 > 0xFFFFFFFEull ? 0xFFFFFFFEu : (uint32_t)e1;
+    for (uint32_t r = 0; r < RF_NR; ++r) h.b0[r] = f2u(st[r]);
+}
+
+// The two binade runs of row quantity r of a half whose start (b0) and
+// step (d) are set: run 0 from the first row, run 1 after one explicit
+// addition (rfd::row_value reads them).  Needed only by triangles
+// rasterised without row records.
+__device__ void half_runs(HalfRec &h, uint32_t r) {
+    uint32_t k0, k1;
+    fast_params(u2f(h.b0[r]), h.d[r], h.i0[r], k0);
+    h.e0[r] = k0;
+    if (k0 == 0xFFFFFFFFu) {  // fixed point: run 0 covers every row
+        h.b1[r] = h.b0[r];
+        h.i1[r] = 0;
+        h.e1[r] = k0;
+        return;
     }
+    const float v1 = fadd(u2f(h.b0[r] + k0 * (uint32_t)h.i0[r]), h.d[r]);
+    fast_params(v1, h.d[r], h.i1[r], k1);
+    h.b1[r] = f2u(v1);
+    const uint64_t e1 = (uint64_t)k0 + 1u + k1;
+    h.e1[r] = e1 > 0xFFFFFFFEull ? 0xFFFFFFFEu : (uint32_t)e1;
 }
 
 }  // namespace
@@ -551,6 +555,10 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     P.rwords = (uint32_t)w;
                     words += (uint32_t)w;
                 }
+                if (P.rwords == 0u) {  // rasterised from this record: it needs the runs
+                    for (int hh = 0; hh < 2; ++hh)
+                        for (uint32_t r = 0; r < RF_NR; ++r) half_runs(P.half[hh], r);
+                }
                 }
             }
             __syncwarp();
@@ -622,7 +630,7 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_
 
 __global__ void __launch_bounds__(256)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
-      const PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev, uint32_t tile_w,
+      PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev, uint32_t tile_w,
       const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
       unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
       StatsDev *__restrict__ stats, uint32_t *__restrict__ counters) {
@@ -696,6 +704,16 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                 if (base + P->rwords > rows_cap) {  // no room: rasterise from the PrimRec
                     regular = false;
                     if (lane == 0) atomicAdd(&counters[RF_CNT_ROWSOVF], 1u);
+                    // ... which then needs its binade runs (lane r: quantity r).
+                    if (lane < RF_NR) {
+                        half_runs(sP->half[0], lane);
+                        half_runs(sP->half[1], lane);
+                    }
+                    __syncwarp();
+                    const uint4 *src = reinterpret_cast<const uint4 *>(sP);
+                    uint4 *dst = reinterpret_cast<uint4 *>(prims + p);
+                    for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) dst[q] = src[q];
+                    __syncwarp();
                 }
             }
             if (lane == 0 && regular) {
