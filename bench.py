@@ -32,6 +32,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W, H, NTRI, SEED = 1920, 1080, 100_000, 2
+# Frames the library's online tiling needs per frame shape before it keeps
+# the fastest tile width (one warm-up + one per width), run before warm-up.
+TUNE_FRAMES = 5
 WORKLOAD = "fill_stress_1080p_100k_gouraud"
 METRIC = "frags/s"
 
@@ -274,6 +277,9 @@ def run_gpu(args):
 
     st = step(sync_stats=True)  # one frame for the per-frame stats
     frags_i, frags_o = st.frags_i, st.frags_o
+    if not args.tile:
+        for _ in range(TUNE_FRAMES):  # online tiling settles (setup, untimed)
+            step()
     for _ in range(args.warmup):
         step()
     dev.sync()
@@ -322,7 +328,9 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded fill-rate stress scene)",
-            "config": config({"tile_w": args.tile or 32, "warps_per_block": args.warps or 4}),
+            "config": config({"tile_w": dev.last_tiling()[0], "warps_per_block": dev.last_tiling()[1],
+                              "tiling": "explicit" if args.tile else
+                              "online per frame shape, settled before the warm-up"}),
             "tris_per_s": NTRI * args.steps * world / (total_ms / 1e3),
             "frames_per_s": args.steps * world / (total_ms / 1e3),
             "frags_o_per_frame": frags_o, "frags_i_per_frame": frags_i,
@@ -462,6 +470,10 @@ def run_workload(args):
             tg.clear()
         rf.render_batch(batch, device=dev, sync_stats=False)
 
+    if not args.tile:
+        for _ in range(TUNE_FRAMES):  # online tiling settles (setup, untimed)
+            step()
+
     if world > 1:
         torch.distributed.barrier()
     step_ms, stage, launches, clk = device_time(dev, stream, step, args.steps, args.warmup,
@@ -490,7 +502,7 @@ def run_workload(args):
             "unit": "frags/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": dict(workloads.describe(name), graphs=graphs,
+            "config": dict(workloads.describe(name), graphs=graphs, tile_w=dev.last_tiling()[0],
                            l2="flushed between steps (512 MiB write)" if flush is not None
                            else "not flushed"),
             "items_per_s": len(scs) * args.steps * world / (total_ms / 1e3),

@@ -116,6 +116,14 @@ const char *rf_status_str(rf_status s);
 /* Tile raster tuning: tile width in pixels (8, 16, 32 or 64; tiles are 32
  * rows high) and rasteriser warps per block.  0 keeps the current value. */
 rf_status rf_ctx_set_tiling(rf_ctx *ctx, uint32_t tile_w, uint32_t warps_per_block);
+/* Online tiling (on by default until rf_ctx_set_tiling sets a tile width):
+ * for each frame shape (draw, scene, vertex and triangle counts, target
+ * pixels) the first frame is a warm-up, the next four run with tile widths
+ * 8, 16, 32 and 64 while CUDA events time their GPU work, and every later
+ * frame of that shape uses the fastest.  Results do not depend on the
+ * width.  rf_ctx_last_tiling reports the last frame's width and warps. */
+rf_status rf_ctx_set_online_tuning(rf_ctx *ctx, int32_t enable);
+rf_status rf_ctx_last_tiling(rf_ctx *ctx, uint32_t *tile_w, uint32_t *warps);
 
 /* Per-stage GPU timing (the device side of Stats::time, stats.rs:57-78).
  * When enabled, every render records CUDA events around its stages on the

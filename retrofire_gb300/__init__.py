@@ -99,6 +99,8 @@ _SIGS = {
     "rf_ctx_sync": [_P],
     "rf_ctx_take_stats": [_P, C.POINTER(CStats)],
     "rf_ctx_set_tiling": [_P, C.c_uint32, C.c_uint32],
+    "rf_ctx_set_online_tuning": [_P, C.c_int32],
+    "rf_ctx_last_tiling": [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
     "rf_mesh_upload": [_P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_uint32,
                        C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint64)],
     "rf_mesh_update": [_P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_uint32)],
@@ -242,6 +244,16 @@ class Device:
 
     def set_tiling(self, tile_w=0, warps=0):
         _check(lib().rf_ctx_set_tiling(self.ptr, tile_w, warps), "rf_ctx_set_tiling")
+
+    def set_online_tuning(self, enable=True):
+        _check(lib().rf_ctx_set_online_tuning(self.ptr, int(bool(enable))),
+               "rf_ctx_set_online_tuning")
+
+    def last_tiling(self):
+        """(tile width, warps per block) of the last frame."""
+        tw, wp = C.c_uint32(), C.c_uint32()
+        _check(lib().rf_ctx_last_tiling(self.ptr, C.byref(tw), C.byref(wp)), "rf_ctx_last_tiling")
+        return tw.value, wp.value
 
     def set_timing(self, enable=True):
         _check(lib().rf_ctx_set_timing(self.ptr, int(bool(enable))), "rf_ctx_set_timing")

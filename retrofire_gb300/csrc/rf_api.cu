@@ -57,6 +57,21 @@ struct GraphEntry {
 };
 constexpr size_t RF_GRAPH_CACHE = 8;
 
+// Online tiling choice for one frame shape: one untimed warm-up frame, then
+// one timed frame per tile width in RF_TUNE_TW, then the fastest width for
+// every later frame of that shape.  All widths give identical results.
+constexpr uint32_t RF_TUNE_TW[4] = {8, 16, 32, 64};
+constexpr size_t RF_TUNE_CACHE = 32;
+struct TuneState {
+    uint64_t key[5];
+    uint32_t next = 0;  // 0: warm-up, 1..4: timed RF_TUNE_TW[next-1], 5: decided
+    int32_t tidx = -1;
+    bool pending = false;
+    float ms[4] = {0, 0, 0, 0};
+    uint32_t best = 32;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
 }  // namespace
 
 struct rf_ctx {
@@ -78,6 +93,10 @@ struct rf_ctx {
     std::vector<GraphEntry> gcache;
     uint64_t gclock = 0, graph_launches = 0;
     uint64_t kernels = 0;  // kernels launched (directly or inside graphs)
+    // Online tiling choice per frame shape (see tune_tile).
+    bool tune_online = true;
+    std::vector<TuneState> tunes;
+    uint32_t last_tile_w = 0;
     // Row-record capacity (words): grown when a frame asked for more, which
     // the library learns from an asynchronous read-back of the total.
     uint64_t rows_cap = 0;
@@ -316,6 +335,74 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
     return RF_OK;
 }
 
+// Tile fields of every job for tile width TW (the jobs were built for
+// another width).
+rf_status retile(std::vector<JobDev> &hj, uint32_t TW) {
+    uint64_t tiles = 0, mask_words = 0;
+    for (JobDev &J : hj) {
+        J.tiles_x = (J.w + TW - 1) / TW;
+        J.tiles_y = (J.h + RF_TILE_H - 1) / RF_TILE_H;
+        J.tile_base = (uint32_t)tiles;
+        J.mask_base = mask_words;
+        tiles += (uint64_t)J.tiles_x * J.tiles_y;
+        mask_words += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
+        if (tiles > 0xFFFFFFF0ull) return RF_ERR_BAD_ARG;
+    }
+    return RF_OK;
+}
+
+// The tile width for this frame (online tuning) and, when the frame is a
+// timed trial, the state whose events bracket its GPU work.
+rf_status tune_tile(rf_ctx *ctx, const uint64_t key[5], uint32_t &TW, TuneState *&timed) {
+    timed = nullptr;
+    TW = ctx->tile_w;
+    if (!ctx->tune_online) return RF_OK;
+    TuneState *ts = nullptr;
+    for (TuneState &t : ctx->tunes)
+        if (memcmp(t.key, key, sizeof t.key) == 0) ts = &t;
+    if (!ts) {
+        if (ctx->tunes.size() >= RF_TUNE_CACHE) {
+            CK(cudaStreamSynchronize(ctx->stream));
+            for (TuneState &t : ctx->tunes) {
+                if (t.e0) cudaEventDestroy(t.e0);
+                if (t.e1) cudaEventDestroy(t.e1);
+            }
+            ctx->tunes.clear();
+        }
+        ctx->tunes.emplace_back();
+        ts = &ctx->tunes.back();
+        memcpy(ts->key, key, sizeof ts->key);
+        CK(cudaEventCreate(&ts->e0));
+        CK(cudaEventCreate(&ts->e1));
+    }
+    if (ts->pending) {
+        CK(cudaEventSynchronize(ts->e1));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, ts->e0, ts->e1));
+        ts->ms[ts->tidx] = ms;
+        ts->pending = false;
+    }
+    if (ts->next == 0) {
+        TW = RF_TUNE_TW[0];
+        ts->next = 1;
+    } else if (ts->next <= 4) {
+        ts->tidx = (int32_t)ts->next - 1;
+        TW = RF_TUNE_TW[ts->tidx];
+        ts->next += 1;
+        timed = ts;
+    } else {
+        if (ts->next == 5) {
+            uint32_t b = 0;
+            for (uint32_t i = 1; i < 4; ++i)
+                if (ts->ms[i] < ts->ms[b]) b = i;
+            ts->best = RF_TUNE_TW[b];
+            ts->next = 6;
+        }
+        TW = ts->best;
+    }
+    return RF_OK;
+}
+
 // One frame: the jobs of `in` (distinct targets), each with its draws in
 // order, as one pass of the pipeline over all of them.  per_job: kernels
 // count into per-job slots (ctx->jstats), folded into the running total at
@@ -336,6 +423,16 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if (hj.empty()) return RF_OK;
     const uint32_t nj = (uint32_t)hj.size();
     if (nj > 1) per_job = true;
+    uint32_t TW = ctx->tile_w;
+    TuneState *tuned = nullptr;
+    {
+        uint64_t px = 0;
+        for (const JobDev &J : hj) px += (uint64_t)J.w * J.h;
+        const uint64_t key[5] = {hd.size(), nj, nv, nt, px};
+        if ((st = tune_tile(ctx, key, TW, tuned))) return st;
+        if (TW != ctx->tile_w && (st = retile(hj, TW))) return st;
+    }
+    ctx->last_tile_w = TW;
     const JobDev &JL = hj.back();
     const uint32_t ntiles = JL.tile_base + JL.tiles_x * JL.tiles_y;
     const size_t mask_words = JL.mask_base + (size_t)JL.tiles_x * JL.tiles_y * JL.mask_words;
@@ -373,7 +470,6 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->rows, ctx->rows_cap * 4))) return st;
 
     cudaStream_t s = ctx->stream;
-    const uint32_t TW = ctx->tile_w;
     int kind = hd[0].shader;
     for (const DrawDev &d : hd)
         if (d.shader != kind) kind = RF_K_ANY;
@@ -438,6 +534,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         return RF_OK;
     };
 
+    if (tuned) CK(cudaEventRecord(tuned->e0, s));
     if (ctx->graphs && !ctx->timing) {
         GraphKey key{};
         const uint64_t kv[] = {ctx->gen, ndraws, nj, nv, nt, ntiles, mask_words, TW, ctx->warps,
@@ -476,6 +573,10 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         ctx->graph_launches += 1;
     } else {
         if ((st = enqueue(ctx->timing))) return st;
+    }
+    if (tuned) {
+        CK(cudaEventRecord(tuned->e1, s));
+        tuned->pending = true;
     }
     // vertex, clip, 3 scan, setup, 3 scan64, bin, raster (+ the stats fold)
     ctx->kernels += 11 + (per_job ? 1 : 0);
@@ -573,6 +674,10 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     for (auto &kv : ctx->textures) cudaFree(kv.second.texels);
     for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); }
     graphs_drop(ctx);
+    for (TuneState &t : ctx->tunes) {
+        if (t.e0) cudaEventDestroy(t.e0);
+        if (t.e1) cudaEventDestroy(t.e1);
+    }
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
@@ -641,8 +746,24 @@ rf_status rf_ctx_set_tiling(rf_ctx *ctx, uint32_t tile_w, uint32_t warps) {
     if (!ctx) return RF_ERR_BAD_ARG;
     if (tile_w && tile_w != 8 && tile_w != 16 && tile_w != 32 && tile_w != 64) return RF_ERR_BAD_ARG;
     if (warps && (warps > RF_RASTER_MAX_THREADS / 32)) return RF_ERR_BAD_ARG;
-    if (tile_w) ctx->tile_w = tile_w;
+    if (tile_w) {
+        ctx->tile_w = tile_w;
+        ctx->tune_online = false;  // an explicit width is kept for every frame
+    }
     if (warps) ctx->warps = warps;
+    return RF_OK;
+}
+
+rf_status rf_ctx_set_online_tuning(rf_ctx *ctx, int32_t enable) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    ctx->tune_online = enable != 0;
+    return RF_OK;
+}
+
+rf_status rf_ctx_last_tiling(rf_ctx *ctx, uint32_t *tile_w, uint32_t *warps) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    if (tile_w) *tile_w = ctx->last_tile_w;
+    if (warps) *warps = ctx->warps;
     return RF_OK;
 }
 
@@ -929,8 +1050,9 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
     rf_status st = read_totals(ctx, before);
     if (st) return st;
     const uint32_t tw0 = ctx->tile_w, wp0 = ctx->warps;
-    const bool timing0 = ctx->timing;
+    const bool timing0 = ctx->timing, online0 = ctx->tune_online;
     ctx->timing = false;
+    ctx->tune_online = false;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto cleanup = [&]() {
         for (Snap &sn : snaps) {
@@ -940,6 +1062,7 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
         ctx->timing = timing0;
+        ctx->tune_online = online0;
     };
     auto restore = [&]() -> cudaError_t {
         for (Snap &sn : snaps) {
@@ -1029,6 +1152,7 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
     add_stats(ctx->taken, d);
     ctx->tile_w = btw;
     ctx->warps = bwp;
+    ctx->tune_online = false;  // the chosen tiling is kept
     if (tile_w) *tile_w = btw;
     if (warps) *warps = bwp;
     if (best_ms) *best_ms = best;

@@ -223,6 +223,7 @@ def test_graph_replay_same_shape():
     equals the oracle (the per-frame matrices travel as data)."""
     dev = rf.Device()
     dev.set_graphs(True)
+    dev.set_online_tuning(False)  # one tile width: one graph
     try:
         for seed in range(30, 36):
             g = cube_spec(seed).alone(dev)
@@ -271,4 +272,24 @@ def test_autotune_leaves_targets_unchanged():
             assert_parity((c, d, st), sp.oracle(), what="scene %d after autotune" % i)
     finally:
         b.close()
+        dev.close()
+
+
+def test_online_tiling_trials_then_keeps_fastest():
+    """Online tiling: a warm-up frame, one timed frame per tile width, then
+    the fastest; every frame equals the oracle."""
+    dev = rf.Device()
+    sp = fill_spec(3000, 400, 300, 61)
+    ref = sp.oracle()
+    seen = []
+    try:
+        for _ in range(8):
+            assert_parity(sp.alone(dev), ref, what="frame %d" % len(seen))
+            seen.append(dev.last_tiling()[0])
+        assert seen[:5] == [8, 8, 16, 32, 64]
+        assert seen[5] in (8, 16, 32, 64) and seen[5] == seen[6] == seen[7]
+        dev.set_tiling(16, 4)  # an explicit width ends the tuning
+        assert_parity(sp.alone(dev), ref)
+        assert dev.last_tiling() == (16, 4)
+    finally:
         dev.close()
