@@ -23,6 +23,19 @@ __device__ __forceinline__ uint32_t upper_index(uint32_t n, uint32_t x, F key) {
     return lo;
 }
 
+// upper_index for the 32 lanes of a warp whose x do not decrease with the
+// lane (all lanes call): one binary search for lane 0's x, then each lane
+// steps forward over the few records between (same result per lane).
+template <class F>
+__device__ __forceinline__ uint32_t warp_upper_index(uint32_t n, uint32_t x, F key) {
+    const uint32_t x0 = __shfl_sync(0xFFFFFFFFu, x, 0);
+    uint32_t d = 0;
+    if ((threadIdx.x & 31) == 0) d = upper_index(n, x0, key);
+    d = __shfl_sync(0xFFFFFFFFu, d, 0);
+    while (d + 1 < n && key(d + 1) <= x) ++d;
+    return d;
+}
+
 // Warp-aggregated 64-bit counter add (all 32 lanes must call).
 __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned long long v,
                                              bool same_dst) {

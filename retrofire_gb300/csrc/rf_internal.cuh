@@ -94,7 +94,8 @@ struct PrimRec {
     int32_t kind;     // shader kind of its draw
     uint32_t rloc;    // word offset of its row records inside its input triangle's block
     uint32_t rwords;  // words of row records; 0 = rasterised from this record instead
-    uint32_t pad_[2];
+    uint32_t job;     // scene (job) of its draw
+    uint32_t pad_;
     HalfRec half[2];
 };
 

@@ -61,9 +61,13 @@ __device__ __forceinline__ uint32_t zdiv_mask_of(int32_t shader) {
 // ---------------------------------------------------------------------------
 __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t nv_total,
                          float4 *__restrict__ cpos, uint8_t *__restrict__ coc) {
-    for (uint32_t gv = blockIdx.x * blockDim.x + threadIdx.x; gv < nv_total;
-         gv += gridDim.x * blockDim.x) {
-        const uint32_t di = upper_index(nd, gv, [&](uint32_t i) { return draws[i].vert_base; });
+    // Warp-uniform loop (the draw lookup is shared by the warp's lanes).
+    for (uint32_t wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wbase < nv_total;
+         wbase += gridDim.x * blockDim.x) {
+        const uint32_t gv = wbase + (threadIdx.x & 31u);
+        const uint32_t di = warp_upper_index(nd, gv < nv_total ? gv : nv_total - 1,
+                                             [&](uint32_t i) { return draws[i].vert_base; });
+        if (gv >= nv_total) continue;
         const DrawDev &d = draws[di];
         const float *src = d.verts + (size_t)(gv - d.vert_base) * d.stride;
         float p[4];
@@ -125,9 +129,13 @@ __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t 
                        uint32_t *__restrict__ tcnt, uint32_t *__restrict__ tpoly,
                        PolyVert *__restrict__ pool, uint32_t pool_cap,
                        uint32_t *__restrict__ counters) {
-    for (uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x; gt < nt_total;
-         gt += gridDim.x * blockDim.x) {
-        const uint32_t di = upper_index(nd, gt, [&](uint32_t i) { return draws[i].tri_base; });
+    // Warp-uniform loop (the draw lookup is shared by the warp's lanes).
+    for (uint32_t wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wbase < nt_total;
+         wbase += gridDim.x * blockDim.x) {
+        const uint32_t gt = wbase + (threadIdx.x & 31u);
+        const uint32_t di = warp_upper_index(nd, gt < nt_total ? gt : nt_total - 1,
+                                             [&](uint32_t i) { return draws[i].tri_base; });
+        if (gt >= nt_total) continue;
         const DrawDev &d = draws[di];
         const uint32_t t = gt - d.tri_base;
         uint32_t vi[3], oc[3];
@@ -462,8 +470,10 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
         uint32_t job = 0xFFFFFFFFu;
         unsigned long long prims_o = 0;
         uint32_t di = 0, t = 0, nc = 0, na = 0, zm = 0, slot = RF_NO_POLY, p0 = 0;
+        const uint32_t dwarp = warp_upper_index(nd, active ? gt : nt_total - 1,
+                                                [&](uint32_t i) { return draws[i].tri_base; });
         if (cnt) {
-            di = upper_index(nd, gt, [&](uint32_t i) { return draws[i].tri_base; });
+            di = dwarp;
             job = draws[di].job;
             t = gt - draws[di].tri_base;
             nc = 1 + nattr_of(draws[di].shader);
@@ -520,6 +530,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 P.kind = d.shader;
                 P.rloc = words;
                 P.rwords = 0;
+                P.job = job;
                 if (!culled) {
                 prims_o += 1;
                 // raster.rs:185-224 tri_fill: stable sort by y (total_cmp).
@@ -638,10 +649,24 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t np = *nprims_dev;
-    __shared__ __align__(16) PrimRec srec[8];  // one per warp of the 256-thread block
+    // Two record slots per warp of the 256-thread block: the next triangle's
+    // record is copied (cp.async) while the current one is walked.
+    __shared__ __align__(16) PrimRec srec[8][2];
     __shared__ __align__(16) RasterPrim srp[8];
     __shared__ float stab[8][32][RF_NR + 1];   // scanline values of one band
-    PrimRec *sP = &srec[wib];
+    auto fetch = [&](PrimRec *dst, uint32_t p) {
+        if (p < np) {
+            const char *src = reinterpret_cast<const char *>(prims + p);
+            for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) {
+                const uint32_t sa = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char *>(dst) + q * 16);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + q * 16)
+                             : "memory");
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    uint32_t cur = 0;
+    fetch(&srec[wib][0], wid);
     RasterPrim *R = &srp[wib];
     float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -669,12 +694,12 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         }
     };
     for (uint32_t p = wid; p < np; p += nw) {
+        __syncwarp();  // the other slot's previous triangle is done
+        fetch(&srec[wib][cur ^ 1u], p + nw);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncwarp();
-        {
-            const uint4 *src = reinterpret_cast<const uint4 *>(prims + p);
-            uint4 *dst = reinterpret_cast<uint4 *>(sP);
-            for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) dst[q] = src[q];
-        }
+        PrimRec *sP = &srec[wib][cur];
+        cur ^= 1u;
         if (lane == 0) {
             R->draw = sP->draw;
             R->flags = sP->live ? RF_RP_LIVE : 0u;
@@ -686,7 +711,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         __syncwarp();
         const PrimRec *P = sP;
         if (P->live) {
-            const uint32_t job = draws[P->draw].job;
+            const uint32_t job = P->job;
             if (job != cur_job) {
                 flush();
                 cur_job = job;
