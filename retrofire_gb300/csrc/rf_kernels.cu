@@ -611,6 +611,15 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
 // ---------------------------------------------------------------------------
 namespace {
 
+// k steps of Iter::next on the first N components, side by side.
+template <int N>
+__device__ __forceinline__ void step_k(float *v, const float *d, uint32_t k) {
+    for (uint32_t i = 0; i < k; ++i) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) v[c] = fadd(v[c], d[c]);
+    }
+}
+
 struct RowOut {
     unsigned long long frags_i;
     uint32_t oob;
@@ -639,7 +648,7 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_
 
 }  // namespace
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
       PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev, uint32_t tile_w,
       const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
@@ -827,9 +836,13 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                                     vb[c] = 0.0f;
                                 }
                             }
-                            for (uint32_t k = 0; k < ksteps; ++k) {
-#pragma unroll
-                                for (uint32_t c = 0; c < RF_NC; ++c) vb[c] = fadd(vb[c], dvc[c]);
+                            switch (nc) {  // only the kind's components step
+                                case 1: step_k<1>(vb, dvc, ksteps); break;
+                                case 2: step_k<2>(vb, dvc, ksteps); break;
+                                case 3: step_k<3>(vb, dvc, ksteps); break;
+                                case 4: step_k<4>(vb, dvc, ksteps); break;
+                                case 5: step_k<5>(vb, dvc, ksteps); break;
+                                default: step_k<6>(vb, dvc, ksteps); break;
                             }
 #pragma unroll
                             for (uint32_t c = 0; c < RF_NC; ++c)
