@@ -47,6 +47,23 @@ def config(extra=None):
     return c
 
 
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time (every rank gets it).  Replicas only: the
+    path has no exchange step, so this is the one collective."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, world, total_ms):
+    """Whole-job rate of `world` replicas that each processed
+    `units_per_rank` units, timed by the slowest rank."""
+    return units_per_rank * world / (total_ms / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -233,7 +250,8 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
         lat.append(time.perf_counter() - t0)
     assert st2.frags_i == frags_i
     lat_ms = sorted(x * 1e3 for x in lat)
-    return {"value": frags_i * args.steps * world / sum(lat), "unit": "frags/s",
+    total_ms = max_over_ranks(1e3 * sum(lat), world, "cuda")
+    return {"value": replica_rate(frags_i * args.steps, world, total_ms), "unit": "frags/s",
             "h2d_bytes_per_step": int(s["verts"].nbytes + s["faces"].nbytes),
             "d2h_bytes_per_step": int(2 * 4 * W * H),
             "latency_ms": {"p50": lat_ms[len(lat_ms) // 2],
@@ -306,13 +324,9 @@ def run_gpu(args):
     step_ms = [a.elapsed_time(b) for a, b in evs]
     stage, nfr = dev.stage_ms()
     dev.set_timing(False)
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), world, "cuda")
     ms = total_ms / args.steps
-    value = frags_i * args.steps * world / (total_ms / 1e3)
+    value = replica_rate(frags_i * args.steps, world, total_ms)
 
     e2e = None
     if not args.no_e2e:
@@ -478,15 +492,12 @@ def run_workload(args):
         torch.distributed.barrier()
     step_ms, stage, launches, clk = device_time(dev, stream, step, args.steps, args.warmup,
                                                 flush, local, stages=not graphs)
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), world, "cuda")
     e2e = None
     if not args.no_e2e:
         e2e = workloads.e2e(objs, dev, args.steps, max(1, args.warmup))
-        e2e["value"] = frags_i * args.steps * world / e2e.pop("seconds")
+        e2e_ms = max_over_ranks(1e3 * e2e.pop("seconds"), world, "cuda")
+        e2e["value"] = replica_rate(frags_i * args.steps, world, e2e_ms)
         e2e["unit"] = "frags/s"
     if rank == 0:
         peak, peak_kind = measured_peak()
@@ -498,7 +509,7 @@ def run_workload(args):
                     "frac": ach / peak, "traffic": None, "kernel": "k_raster",
                     "peak_kind": peak_kind, "alg_bytes_per_launch": alg}
         line = {
-            "metric": METRIC, "value": frags_i * args.steps * world / (total_ms / 1e3),
+            "metric": METRIC, "value": replica_rate(frags_i * args.steps, world, total_ms),
             "unit": "frags/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
