@@ -261,6 +261,26 @@ rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint32_t pos_di
                             const uint32_t *clear_rgba, const float *depth_clear,
                             void *cuda_stream, rf_stats *stats);
 
+/* ---- mesh ingestion (Wavefront OBJ) -----------------------------------
+ * retrofire's OBJ reader (geom/src/io.rs:106-370) as a host function: v,
+ * vt, vn and f (triangles; quads split as [a,b,c], [a,c,d]); comments, g,
+ * mtllib, usemtl and s skipped; any other item, a missing token, a bad
+ * number, an out-of-range or zero index, a missing attribute kind or faces
+ * that mix with and without normals/texcoords return RF_ERR_BAD_ARG with a
+ * message in err.  Vertices are the distinct (position, texcoord, normal)
+ * index triples in order of first use, like Mesh::new via the reader's
+ * Builder.  attrs picks the vertex attributes: positions only (nattr 0),
+ * normals (3), texcoords (2) or normal + texcoord (5).  *verts (nverts *
+ * (3 + nattr) floats) and *idx (3 * ntri u32) are allocated by the library;
+ * release them with rf_obj_free.  Needs no GPU. */
+enum { RF_OBJ_POSITION = 0, RF_OBJ_NORMAL = 1, RF_OBJ_TEXCOORD = 2, RF_OBJ_NORMAL_TEXCOORD = 3 };
+rf_status rf_obj_parse(const char *text, size_t len, int32_t attrs, float **verts, uint32_t *nverts,
+                       uint32_t *nattr, uint32_t **idx, uint32_t *ntri, char *err, size_t err_len);
+void rf_obj_free(void *p);
+/* rf_obj_parse, then rf_mesh_upload of the result (positions in model
+ * space, pos_dim 3). */
+rf_status rf_mesh_load_obj(rf_ctx *ctx, const char *text, size_t len, int32_t attrs, rf_mesh *out);
+
 /* ---- serving loop -----------------------------------------------------
  * No counterpart in the reference, which renders one frame per call on
  * the caller's thread (render.rs:134).  A server takes over an rf_ctx

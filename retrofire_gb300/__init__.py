@@ -36,6 +36,7 @@ CULL_NONE, CULL_BACK, CULL_FRONT = range(3)
 NATTR = {FLAT: 0, GOURAUD: 3, TEXTURED: 2, TEX_GOURAUD: 5, GOURAUD_SRGB: 3}
 
 STAGES = ("vertex", "clip", "scan", "setup", "raster")
+OBJ_POSITION, OBJ_NORMAL, OBJ_TEXCOORD, OBJ_NORMAL_TEXCOORD = range(4)
 
 STATUS = {0: "ok", 1: "bad handle", 2: "bad argument", 3: "non power-of-two texture",
           4: "out of device memory", 5: "over budget", 6: "overflow", 7: "timeout",
@@ -129,6 +130,10 @@ _SIGS = {
     "rf_server_wait": [_P, C.c_uint64, C.c_uint32, C.POINTER(Result)],
     "rf_server_counts": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
     "rf_server_destroy": [_P],
+    "rf_obj_parse": [C.c_char_p, C.c_size_t, C.c_int32, C.POINTER(C.POINTER(C.c_float)),
+                     C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_uint32)),
+                     C.POINTER(C.c_uint32), C.c_char_p, C.c_size_t],
+    "rf_mesh_load_obj": [_P, C.c_char_p, C.c_size_t, C.c_int32, C.POINTER(C.c_uint64)],
     "rf_ctx_set_graphs": [_P, C.c_int32],
     "rf_ctx_counts": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)],
     "rf_ctx_autotune": [_P, C.POINTER(Job), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
@@ -158,6 +163,8 @@ def lib():
             fn.restype = C.c_int32
         L.rf_status_str.argtypes = [C.c_int32]
         L.rf_status_str.restype = C.c_char_p
+        L.rf_obj_free.argtypes = [_P]
+        L.rf_obj_free.restype = None
         _lib = L
     return _lib
 
@@ -623,3 +630,32 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class ObjError(ValueError):
+    pass
+
+
+def parse_obj(text, attrs=OBJ_POSITION):
+    """Wavefront OBJ text (str or bytes) -> (verts (n, 3 + nattr) float32,
+    faces (m, 3) uint32), like retrofire's reader (geom/src/io.rs).  Runs
+    in the library on the host; raises ObjError with the reader's message."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    vp, ip = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
+    nv, na, nt = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    err = C.create_string_buffer(256)
+    code = lib().rf_obj_parse(data, len(data), attrs, C.byref(vp), C.byref(nv), C.byref(na),
+                              C.byref(ip), C.byref(nt), err, 256)
+    if code == 2 and err.value:
+        raise ObjError(err.value.decode())
+    _check(code, "rf_obj_parse")
+    try:
+        w = 3 + na.value
+        verts = np.ctypeslib.as_array(vp, (nv.value * w,)).copy().reshape(nv.value, w) \
+            if nv.value else np.zeros((0, w), np.float32)
+        faces = np.ctypeslib.as_array(ip, (nt.value * 3,)).copy().reshape(nt.value, 3) \
+            if nt.value else np.zeros((0, 3), np.uint32)
+    finally:
+        lib().rf_obj_free(C.cast(vp, _P))
+        lib().rf_obj_free(C.cast(ip, _P))
+    return verts, faces

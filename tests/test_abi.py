@@ -37,7 +37,7 @@ def test_library_exports_all_declared(libpath):
 
 
 def test_python_bindings_cover_header(libpath):
-    bound = set(rf._SIGS) | {"rf_status_str"}
+    bound = set(rf._SIGS) | {"rf_status_str", "rf_obj_free"}
     assert set(declared_symbols()) <= bound, set(declared_symbols()) - bound
 
 
