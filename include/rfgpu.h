@@ -87,16 +87,28 @@ typedef struct {
 } rf_context_flags;
 
 /* Stats / Throughput (render/stats.rs:16-40).  oob counts scanlines that
- * left the target buffer (where the reference would panic). */
+ * left the target buffer (where the reference would panic).  objs_i /
+ * objs_o: draws submitted with RF_DRAW_CULL_BBOX and those of them drawn
+ * (Stats::objs as the per-object loop of demos/src/bin/crates.rs:114-133
+ * keeps it). */
 typedef struct {
     uint64_t calls, prims_i, prims_o, verts_i, verts_o, frags_i, frags_o, oob;
+    uint64_t objs_i, objs_o;
 } rf_stats;
 
-/* One render() call for rf_render_draws (Batch::render, batch.rs:127-146). */
+/* One render() call for rf_render_draws (Batch::render, batch.rs:127-146).
+ * flags: RF_DRAW_CULL_BBOX = object-level frustum culling of the
+ * per-object loop (crates.rs:114-133): when the mesh's bounding box
+ * (BBox::of its positions, render/scene.rs:37-39) is Hidden under the
+ * draw's mvp (BBox::visibility, scene.rs:80-87: the 8 corners through the
+ * vertex transform, their outcodes, view_frustum::status, clip.rs:245-267)
+ * the draw is skipped like a render() call that was never made; every
+ * other draw renders as without the flag.  Meshes with pos_dim 3 only. */
+#define RF_DRAW_CULL_BBOX 1u
 typedef struct {
     rf_mesh mesh;
     int32_t shader;
-    int32_t pad_;
+    uint32_t flags;
     rf_uniforms uniforms;
 } rf_draw;
 

@@ -59,6 +59,8 @@ def lib():
         L.rfo_tri_fill.restype = C.c_uint32
         L.rfo_sample.argtypes = [u32p, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, C.c_float]
         L.rfo_sample.restype = C.c_uint32
+        L.rfo_bbox_status.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
+        L.rfo_bbox_status.restype = C.c_int32
         _lib = L
     return _lib
 
@@ -156,3 +158,14 @@ def sample(tex, sampler, u, v):
 
 __all__ = ["Draw", "Ctx", "Stats", "make_draw", "render", "clear", "pack",
            "clip_batch", "tri_fill", "sample", "lib"]
+
+
+VISIBLE, CLIPPED, HIDDEN = 0, 1, 2
+
+
+def bbox_status(verts, mvp, pos_dim=3):
+    """BBox::of the positions, then BBox::visibility under mvp (scene.rs):
+    VISIBLE, CLIPPED or HIDDEN."""
+    v = np.ascontiguousarray(verts, np.float32)
+    m = np.ascontiguousarray(mvp, np.float32).reshape(-1)
+    return int(lib().rfo_bbox_status(_fp(v), v.shape[0], v.shape[1], _fp(m)))

@@ -360,6 +360,31 @@ constexpr uint32_t zdiv_mask() {
 }  // namespace
 
 // pixfmt.rs:76-103: u32::from_be_bytes of the format's byte order.
+// render/scene.rs BBox::of (:37-39, extend :42-46: f32::min / f32::max
+// from the empty box), BBox::verts (:60-67) and BBox::visibility (:80-87):
+// the corners through the vertex transform (mat.rs:952-973), ClipVert::new
+// outcodes and view_frustum::status (clip.rs:245-267).  Returns 0 Visible,
+// 1 Clipped, 2 Hidden.
+extern "C" int32_t rfo_bbox_status(const float *verts, uint32_t nverts, uint32_t stride,
+                                   const float mvp[16]) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < nverts; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::fmin(lo[k], verts[(uint64_t)i * stride + k]);
+            hi[k] = std::fmax(hi[k], verts[(uint64_t)i * stride + k]);
+        }
+    uint8_t all = 0xFF, any = 0;
+    for (int c = 0; c < 8; ++c) {
+        const float hom[4] = {(c & 4) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 1) ? hi[2] : lo[2], 1.0f};
+        float p[4];
+        for (int k = 0; k < 4; ++k) p[k] = dot4(mvp + 4 * k, hom);
+        const uint8_t oc = outcode(p);
+        all &= oc;
+        any |= oc;
+    }
+    return all != 0 ? 2 : (any == 0 ? 0 : 1);
+}
+
 extern "C" uint32_t rfo_pack(uint32_t c, int32_t fmt) {
     uint32_t r = c & 0xFF, g = (c >> 8) & 0xFF, b = (c >> 16) & 0xFF, a = c >> 24;
     switch (fmt) {

@@ -61,11 +61,15 @@ class Flags(C.Structure):
 
 class CStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("calls", "prims_i", "prims_o", "verts_i", "verts_o",
-                                          "frags_i", "frags_o", "oob")]
+                                          "frags_i", "frags_o", "oob", "objs_i", "objs_o")]
+
+
+# rf_draw flags
+DRAW_CULL_BBOX = 1
 
 
 class Draw(C.Structure):
-    _fields_ = [("mesh", C.c_uint64), ("shader", C.c_int32), ("pad_", C.c_int32),
+    _fields_ = [("mesh", C.c_uint64), ("shader", C.c_int32), ("flags", C.c_uint32),
                 ("uniforms", Uniforms)]
 
 
@@ -184,7 +188,8 @@ def _u32p(a):
 
 class Stats:
     """Stats (stats.rs:16-40): calls and per-stage Throughput in/out."""
-    FIELDS = ("calls", "prims_i", "prims_o", "verts_i", "verts_o", "frags_i", "frags_o", "oob")
+    FIELDS = ("calls", "prims_i", "prims_o", "verts_i", "verts_o", "frags_i", "frags_o", "oob",
+              "objs_i", "objs_o")
 
     def __init__(self, **kw):
         for f in self.FIELDS:
@@ -452,12 +457,15 @@ def render(prims, verts, shader, uniform, to_screen, target, ctx=None, pos_dim=3
 def render_draws(draws, to_screen, target, ctx=None, sync_stats=True):
     """Several render() calls into one target, in order, as one GPU pass.
 
-    draws: list of (Mesh, Shader, mvp)."""
+    draws: list of (Mesh, Shader, mvp) or (Mesh, Shader, mvp, flags), flags
+    DRAW_CULL_BBOX for object-level frustum culling."""
     ctx = ctx or Context()
     arr = (Draw * len(draws))()
-    for i, (mesh, shader, mvp) in enumerate(draws):
+    for i, dr in enumerate(draws):
+        mesh, shader, mvp = dr[:3]
         arr[i].mesh = mesh.handle
         arr[i].shader = shader.kind
+        arr[i].flags = dr[3] if len(dr) > 3 else 0
         arr[i].uniforms = shader.uniforms(mvp)
     vp = np.ascontiguousarray(to_screen, np.float32).reshape(-1)
     fl = ctx.flags()
@@ -490,9 +498,11 @@ class Scene:
             arr = (Draw * max(1, len(self.draws)))()
             if self.draws:
                 mvps = np.zeros((len(self.draws), 16), np.float32)
-                for i, (mesh, shader, mvp) in enumerate(self.draws):
+                for i, dr in enumerate(self.draws):
+                    mesh, shader, mvp = dr[:3]
                     arr[i].mesh = mesh.handle
                     arr[i].shader = shader.kind
+                    arr[i].flags = dr[3] if len(dr) > 3 else 0
                     arr[i].uniforms = shader.uniforms(None)
                     if mvp is not None:
                         mvps[i] = np.asarray(mvp, np.float32).reshape(-1)
@@ -579,9 +589,11 @@ class Server:
         that receive the image (allocated here when None)."""
         ctx = ctx or Context()
         arr = (Draw * max(1, len(draws)))()
-        for i, (mesh, shader, mvp) in enumerate(draws):
+        for i, dr in enumerate(draws):
+            mesh, shader, mvp = dr[:3]
             arr[i].mesh = mesh.handle
             arr[i].shader = shader.kind
+            arr[i].flags = dr[3] if len(dr) > 3 else 0
             arr[i].uniforms = shader.uniforms(mvp)
         if color_out is None:
             color_out = np.empty((h, w), np.uint32)

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -24,7 +25,24 @@ struct Mesh {
     float *verts = nullptr;
     uint32_t *idx = nullptr;
     uint32_t nverts = 0, ntri = 0, pos_dim = 3, nattr = 0;
+    // BBox::of the positions (render/scene.rs:37-39): low x,y,z, high x,y,z
+    float bbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
 };
+
+// BBox::extend over every position (f32::min / f32::max, scene.rs:42-46).
+void mesh_bbox(Mesh &m, const float *verts) {
+    for (int k = 0; k < 3; ++k) {
+        m.bbox[k] = INFINITY;
+        m.bbox[3 + k] = -INFINITY;
+    }
+    const uint32_t stride = m.pos_dim + m.nattr;
+    for (uint32_t i = 0; i < m.nverts; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const float x = verts[(size_t)i * stride + k];
+            m.bbox[k] = fminf(m.bbox[k], x);
+            m.bbox[3 + k] = fmaxf(m.bbox[3 + k], x);
+        }
+}
 struct Texture {
     uint32_t *texels = nullptr;
     uint32_t w = 0, h = 0;
@@ -180,7 +198,16 @@ uint32_t pack_px(uint32_t c, int32_t fmt) {
 void add_stats(rf_stats &a, const rf_stats &b) {
     a.calls += b.calls; a.prims_i += b.prims_i; a.prims_o += b.prims_o;
     a.verts_i += b.verts_i; a.verts_o += b.verts_o; a.frags_i += b.frags_i;
-    a.frags_o += b.frags_o; a.oob += b.oob;
+    a.frags_o += b.frags_o; a.oob += b.oob; a.objs_i += b.objs_i; a.objs_o += b.objs_o;
+}
+
+rf_stats sub_stats(const rf_stats &a, const rf_stats &b) {
+    rf_stats d{};
+    d.calls = a.calls - b.calls; d.prims_i = a.prims_i - b.prims_i; d.prims_o = a.prims_o - b.prims_o;
+    d.verts_i = a.verts_i - b.verts_i; d.verts_o = a.verts_o - b.verts_o;
+    d.frags_i = a.frags_i - b.frags_i; d.frags_o = a.frags_o - b.frags_o; d.oob = a.oob - b.oob;
+    d.objs_i = a.objs_i - b.objs_i; d.objs_o = a.objs_o - b.objs_o;
+    return d;
 }
 
 // Device stats + overflow counters + host counts = the running total.
@@ -196,6 +223,12 @@ rf_status read_totals(rf_ctx *ctx, rf_stats &tot) {
     tot.frags_i += sd.frags_i;
     tot.frags_o += sd.frags_o;
     tot.oob += sd.oob + cnt[RF_CNT_POOLOVF] + cnt[RF_CNT_POLYOVF] + cnt[RF_CNT_BADIDX];
+    // culled draws are render() calls that were not made
+    tot.calls -= sd.cull_calls;
+    tot.prims_i -= sd.cull_prims;
+    tot.verts_i -= sd.cull_verts;
+    tot.objs_i += sd.objs_i;
+    tot.objs_o += sd.objs_o;
     return RF_OK;
 }
 
@@ -285,6 +318,9 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
             d.vert_base = (uint32_t)nv;
             d.tri_base = (uint32_t)nt;
             d.job = (uint32_t)hj.size();
+            d.flags = dr.flags & RF_DRAW_CULL_BBOX;
+            d.culled = 0;
+            memcpy(d.bbox, m.bbox, sizeof d.bbox);
             memcpy(d.mvp, dr.uniforms.mvp, sizeof d.mvp);
             nv += m.nverts;
             nt += m.ntri;
@@ -471,8 +507,11 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
 
     cudaStream_t s = ctx->stream;
     int kind = hd[0].shader;
-    for (const DrawDev &d : hd)
+    bool any_cull = false;
+    for (const DrawDev &d : hd) {
         if (d.shader != kind) kind = RF_K_ANY;
+        any_cull = any_cull || (d.flags & RF_DRAW_CULL_BBOX);
+    }
     bool fast = true;
     for (const JobDev &J : hj)
         fast = fast && J.depth && J.depth_test == RF_DEPTH_LESS && J.color_write && J.depth_write;
@@ -507,6 +546,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(cudaMemsetAsync(ctx->mask.p, 0, mask_words * 4, s));
         if (per_job) CK(cudaMemsetAsync(kst, 0, nj * sizeof(StatsDev), s));
         CK(mark(RF_STAGE_VERTEX));
+        if (any_cull) CK(rfk::launch_cull(P<DrawDev>(ctx->draws), ndraws, kst, ctx->nsm, s));
         CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
                               ctx->nsm, s));
         CK(mark(RF_STAGE_CLIP));
@@ -538,7 +578,8 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if (ctx->graphs && !ctx->timing) {
         GraphKey key{};
         const uint64_t kv[] = {ctx->gen, ndraws, nj, nv, nt, ntiles, mask_words, TW, ctx->warps,
-                               (uint64_t)(kind + 16), fast ? 1u : 0u, per_job ? 1u : 0u, ctx->rows_cap};
+                               (uint64_t)(kind + 16) | (any_cull ? 0x100u : 0u), fast ? 1u : 0u,
+                               per_job ? 1u : 0u, ctx->rows_cap};
         static_assert(sizeof kv == sizeof key.v, "graph key size");
         memcpy(key.v, kv, sizeof kv);
         GraphEntry *hit = nullptr;
@@ -579,7 +620,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         tuned->pending = true;
     }
     // vertex, clip, 3 scan, setup, 3 scan64, bin, raster (+ the stats fold)
-    ctx->kernels += 11 + (per_job ? 1 : 0);
+    ctx->kernels += 11 + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -605,15 +646,7 @@ rf_status finish_call(rf_ctx *ctx, rf_stats *out) {
     rf_stats tot{};
     rf_status st = read_totals(ctx, tot);
     if (st) return st;
-    rf_stats d{};
-    d.calls = tot.calls - ctx->taken.calls;
-    d.prims_i = tot.prims_i - ctx->taken.prims_i;
-    d.prims_o = tot.prims_o - ctx->taken.prims_o;
-    d.verts_i = tot.verts_i - ctx->taken.verts_i;
-    d.verts_o = tot.verts_o - ctx->taken.verts_o;
-    d.frags_i = tot.frags_i - ctx->taken.frags_i;
-    d.frags_o = tot.frags_o - ctx->taken.frags_o;
-    d.oob = tot.oob - ctx->taken.oob;
+    const rf_stats d = sub_stats(tot, ctx->taken);
     ctx->taken = tot;
     *out = d;
     return RF_OK;
@@ -784,6 +817,7 @@ rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint3
     if (vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
     if (ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    mesh_bbox(m, verts);
     const uint64_t h = ctx->next_handle++;
     ctx->meshes[h] = m;
     *out = h;
@@ -802,6 +836,7 @@ rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const ui
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (verts) mesh_bbox(m, verts);
     return RF_OK;
 }
 
@@ -999,6 +1034,11 @@ rf_status rf_render_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, rf_st
             o.frags_i = d.frags_i;
             o.frags_o = d.frags_o;
             o.oob = d.oob;
+            o.calls -= d.cull_calls;
+            o.prims_i -= d.cull_prims;
+            o.verts_i -= d.cull_verts;
+            o.objs_i = d.objs_i;
+            o.objs_o = d.objs_o;
         }
         stats[k] = o;
         add_stats(ctx->taken, o);
@@ -1140,16 +1180,7 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
         return st;
     }
     // The trial renders are not the caller's: hide their stats.
-    rf_stats d{};
-    d.calls = after.calls - before.calls;
-    d.prims_i = after.prims_i - before.prims_i;
-    d.prims_o = after.prims_o - before.prims_o;
-    d.verts_i = after.verts_i - before.verts_i;
-    d.verts_o = after.verts_o - before.verts_o;
-    d.frags_i = after.frags_i - before.frags_i;
-    d.frags_o = after.frags_o - before.frags_o;
-    d.oob = after.oob - before.oob;
-    add_stats(ctx->taken, d);
+    add_stats(ctx->taken, sub_stats(after, before));
     ctx->tile_w = btw;
     ctx->warps = bwp;
     ctx->tune_online = false;  // the chosen tiling is kept

@@ -33,6 +33,9 @@ struct DrawDev {
     uint32_t vert_base;  // first global vertex of this draw
     uint32_t tri_base;   // first global input triangle of this draw
     uint32_t job;
+    uint32_t flags;   // RF_DRAW_CULL_BBOX
+    uint32_t culled;  // set on the device: the draw's bbox is Hidden
+    float bbox[6];    // BBox::of the positions: low x,y,z, high x,y,z
     float mvp[16];
 };
 
@@ -55,6 +58,9 @@ struct JobDev {
 
 struct StatsDev {
     unsigned long long prims_o, verts_o, frags_i, frags_o, oob;
+    // object culling: draws tested / drawn, and the host counts of the
+    // culled draws (taken back out of calls, prims_i, verts_i)
+    unsigned long long objs_i, objs_o, cull_calls, cull_prims, cull_verts;
 };
 
 struct PolyVert {

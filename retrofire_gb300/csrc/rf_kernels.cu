@@ -69,6 +69,7 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
                                              [&](uint32_t i) { return draws[i].vert_base; });
         if (gv >= nv_total) continue;
         const DrawDev &d = draws[di];
+        if (d.culled) continue;  // a render() call that is not made
         const float *src = d.verts + (size_t)(gv - d.vert_base) * d.stride;
         float p[4];
         if (d.pos_dim == 4) {
@@ -80,6 +81,39 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
         }
         cpos[gv] = make_float4(p[0], p[1], p[2], p[3]);
         coc[gv] = (uint8_t)outcode(p);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K0: object-level frustum culling (render/scene.rs:80-87 BBox::visibility
+// as the per-object loop of demos/src/bin/crates.rs:114-133 uses it): one
+// thread per draw with RF_DRAW_CULL_BBOX.  The bbox corners in BBox::verts
+// order go through the draw's vertex transform; all eight outside one plane
+// (view_frustum::status == Hidden, clip.rs:245-267) culls the draw.
+// ---------------------------------------------------------------------------
+__global__ void k_cull(DrawDev *__restrict__ draws, uint32_t nd, StatsDev *__restrict__ stats) {
+    for (uint32_t di = blockIdx.x * blockDim.x + threadIdx.x; di < nd; di += gridDim.x * blockDim.x) {
+        DrawDev &d = draws[di];
+        d.culled = 0;
+        if (!(d.flags & RF_K_DRAW_CULL_BBOX) || d.pos_dim != 3) continue;
+        uint32_t all = 0x3Fu;
+        for (int c = 0; c < 8; ++c) {
+            const float h[4] = {d.bbox[(c & 4) ? 3 : 0], d.bbox[(c & 2) ? 4 : 1], d.bbox[(c & 1) ? 5 : 2], 1.0f};
+            float p[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) p[r] = dot4(d.mvp + 4 * r, h);
+            all &= outcode(p);
+        }
+        StatsDev &S = stats[d.job];
+        atomicAdd(&S.objs_i, 1ull);
+        if (all) {
+            d.culled = 1;
+            atomicAdd(&S.cull_calls, 1ull);
+            atomicAdd(&S.cull_prims, (unsigned long long)d.ntri);
+            atomicAdd(&S.cull_verts, (unsigned long long)d.nverts);
+        } else {
+            atomicAdd(&S.objs_o, 1ull);
+        }
     }
 }
 
@@ -137,6 +171,11 @@ __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t 
                                              [&](uint32_t i) { return draws[i].tri_base; });
         if (gt >= nt_total) continue;
         const DrawDev &d = draws[di];
+        if (d.culled) {  // a render() call that is not made: no output
+            tcnt[gt] = 0;
+            tpoly[gt] = RF_NO_POLY;
+            continue;
+        }
         const uint32_t t = gt - d.tri_base;
         uint32_t vi[3], oc[3];
         bool bad = false;
@@ -996,36 +1035,43 @@ cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jo
     }
 }
 
+cudaError_t launch_cull(DrawDev *draws, uint32_t nd, StatsDev *stats, int nsm, cudaStream_t s) {
+    if (nd == 0) return cudaSuccess;
+    const uint32_t blocks = min((nd + 127) / 128, (uint32_t)nsm * 8);
+    k_cull<<<blocks, 128, 0, s>>>(draws, nd, stats);
+    return cudaGetLastError();
+}
+
 // Per-job stats of a batch folded into the context's running total.  One
 // block; stream order makes the plain read-modify-write of *total safe.
 __global__ void __launch_bounds__(256) k_stats_fold(const StatsDev *__restrict__ js, uint32_t n,
                                                     StatsDev *__restrict__ total) {
-    __shared__ unsigned long long part[5][8];
-    unsigned long long a[5] = {0, 0, 0, 0, 0};
+    constexpr int NF = (int)(sizeof(StatsDev) / sizeof(unsigned long long));
+    static_assert(sizeof(StatsDev) == NF * sizeof(unsigned long long), "StatsDev is all counters");
+    __shared__ unsigned long long part[NF][8];
+    unsigned long long a[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) a[f] = 0;
     for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-        a[0] += js[j].prims_o;
-        a[1] += js[j].verts_o;
-        a[2] += js[j].frags_i;
-        a[3] += js[j].frags_o;
-        a[4] += js[j].oob;
+        const unsigned long long *c = reinterpret_cast<const unsigned long long *>(js + j);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) a[f] += c[f];
     }
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int f = 0; f < 5; ++f) {
+    for (int f = 0; f < NF; ++f) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a[f] += __shfl_xor_sync(0xFFFFFFFFu, a[f], o);
         if (lane == 0) part[f][w] = a[f];
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long t[5] = {0, 0, 0, 0, 0};
-        for (uint32_t i = 0; i < blockDim.x / 32; ++i)
-            for (int f = 0; f < 5; ++f) t[f] += part[f][i];
-        total->prims_o += t[0];
-        total->verts_o += t[1];
-        total->frags_i += t[2];
-        total->frags_o += t[3];
-        total->oob += t[4];
+        unsigned long long *t = reinterpret_cast<unsigned long long *>(total);
+        for (int f = 0; f < NF; ++f) {
+            unsigned long long sum = 0;
+            for (uint32_t i = 0; i < blockDim.x / 32; ++i) sum += part[f][i];
+            t[f] += sum;
+        }
     }
 }
 

@@ -29,6 +29,7 @@
 #define RF_K_CULL_NONE 0
 #define RF_K_CULL_BACK 1
 #define RF_K_CULL_FRONT 2
+#define RF_K_DRAW_CULL_BBOX 1u
 
 #define RF_NO_POLY 0xFFFFFFFFu
 // Scanline y origins beyond +-2^22 px are outside the supported domain: the
@@ -90,6 +91,9 @@ RF_DECL_RASTER_TW(64)
 #undef RF_DECL_RASTER_TW
 cudaError_t launch_fill(uint32_t *color, float *depth, size_t n, uint32_t px, float z,
                         uint32_t flags, int nsm, cudaStream_t s);
+// Object culling of the draws with RF_DRAW_CULL_BBOX (sets DrawDev::culled
+// and counts into stats[draw.job]).
+cudaError_t launch_cull(DrawDev *draws, uint32_t nd, StatsDev *stats, int nsm, cudaStream_t s);
 // Adds the n per-job stats slots js[0..n) into *total (one block).
 cudaError_t launch_stats_fold(const StatsDev *js, uint32_t n, StatsDev *total, cudaStream_t s);
 }  // namespace rfk

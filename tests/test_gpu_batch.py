@@ -192,8 +192,8 @@ def test_batch_stats_accumulate_without_sync():
         for sp in specs:
             for k, v in sp.oracle()[2].items():
                 exp[k] = exp.get(k, 0) + v
-        assert tot == exp
-        assert dev.take_stats().as_dict() == {k: 0 for k in exp}
+        assert tot == dict(exp, objs_i=0, objs_o=0)
+        assert dev.take_stats().as_dict() == {k: 0 for k in tot}
     finally:
         b.close()
         dev.close()
