@@ -120,7 +120,8 @@ rf_status rf_ctx_destroy(rf_ctx *ctx);
 /* The CUDA device the context was created on (the caller's current device
  * at rf_ctx_create). */
 rf_status rf_ctx_device(rf_ctx *ctx, int32_t *device);
-/* Waits for all work queued on the context's stream. */
+/* Waits for all work queued on the context's streams (rendering and the
+ * streaming copies). */
 rf_status rf_ctx_sync(rf_ctx *ctx);
 /* Adds the stats of every render since the last call into *out (and syncs). */
 rf_status rf_ctx_take_stats(rf_ctx *ctx, rf_stats *out);
@@ -159,6 +160,14 @@ rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint3
 /* Replaces the contents of a mesh with arrays of the same sizes (an
  * animated or re-submitted mesh without reallocation). */
 rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx);
+/* Streaming variants: the copies run on the context's own upload / read-back
+ * streams and return at once.  A render that reads the mesh waits for its
+ * upload; an upload waits for every queued render that reads the mesh; a
+ * read waits for every queued render into the target; the next render into
+ * the target (or write, clear) waits for the read.  The host buffers must
+ * stay valid (and, for a read, unread) until rf_ctx_sync; page-locked host
+ * memory lets the copies overlap the rendering of other frames. */
+rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx);
 /* Sizes of a mesh; NULL pointers are skipped. */
 rf_status rf_mesh_info(rf_ctx *ctx, rf_mesh mesh, uint32_t *nverts, uint32_t *ntri, uint32_t *nattr);
 rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh);
@@ -182,6 +191,8 @@ rf_status rf_target_clear(rf_ctx *ctx, rf_target t, const uint32_t *clear_rgba,
 rf_status rf_target_write(rf_ctx *ctx, rf_target t, const uint32_t *color, const float *depth);
 /* Copies the target to host memory (synchronous); NULL skips a buffer. */
 rf_status rf_target_read(rf_ctx *ctx, rf_target t, uint32_t *color, float *depth);
+/* See rf_mesh_update_async. */
+rf_status rf_target_read_async(rf_ctx *ctx, rf_target t, uint32_t *color, float *depth);
 
 /* ---- rendering -------------------------------------------------------- */
 /* render(mesh.faces, mesh.verts, shader, uniforms, viewport, target, ctx)

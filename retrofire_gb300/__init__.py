@@ -109,6 +109,8 @@ _SIGS = {
     "rf_mesh_upload": [_P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_uint32,
                        C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint64)],
     "rf_mesh_update": [_P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_uint32)],
+    "rf_mesh_update_async": [_P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_uint32)],
+    "rf_target_read_async": [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_float)],
     "rf_mesh_destroy": [_P, C.c_uint64],
     "rf_ctx_set_timing": [_P, C.c_int32],
     "rf_ctx_stage_ms": [_P, C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
@@ -329,6 +331,14 @@ class Mesh:
         _check(lib().rf_mesh_update(self.dev.ptr, self.handle, _fp(v) if v is not None else None,
                                     _u32p(f) if f is not None else None), "rf_mesh_update")
 
+    def update_async(self, verts=None, faces=None):
+        """rf_mesh_update_async: the arrays must stay alive and unchanged
+        until Device.sync (page-locked memory for overlap)."""
+        _check(lib().rf_mesh_update_async(self.dev.ptr, self.handle,
+                                          _fp(verts) if verts is not None else None,
+                                          _u32p(faces) if faces is not None else None),
+               "rf_mesh_update_async")
+
     def close(self):
         if self.handle and self.dev.ptr:
             lib().rf_mesh_destroy(self.dev.ptr, self.handle)
@@ -386,6 +396,13 @@ class Framebuf:
         _check(lib().rf_target_read(self.dev.ptr, self.handle, _u32p(color),
                                     _fp(depth) if depth is not None else None), "rf_target_read")
         return color, depth
+
+    def read_async(self, color, depth=None):
+        """rf_target_read_async into caller arrays (h, w) uint32 / float32;
+        valid after Device.sync."""
+        _check(lib().rf_target_read_async(self.dev.ptr, self.handle, _u32p(color),
+                                          _fp(depth) if depth is not None else None),
+               "rf_target_read_async")
 
     def close(self):
         if self.handle and self.dev.ptr:

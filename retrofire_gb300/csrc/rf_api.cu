@@ -27,6 +27,10 @@ struct Mesh {
     uint32_t nverts = 0, ntri = 0, pos_dim = 3, nattr = 0;
     // BBox::of the positions (render/scene.rs:37-39): low x,y,z, high x,y,z
     float bbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    // Asynchronous updates (rf_mesh_update_async): `used` marks the last
+    // render that read the mesh, `ready` the end of the last upload.
+    bool async = false, ready_pending = false;
+    cudaEvent_t used = nullptr, ready = nullptr;
 };
 
 // BBox::extend over every position (f32::min / f32::max, scene.rs:42-46).
@@ -55,6 +59,10 @@ struct Target {
     uint32_t clear_flags = 0;  // pending Frame::clear, fused into the next render
     uint32_t clear_px = 0;
     float clear_z = 0.0f;
+    // Asynchronous reads (rf_target_read_async): `rendered` marks the last
+    // work that wrote the target, `read_done` the end of the last read.
+    bool async = false, read_pending = false;
+    cudaEvent_t rendered = nullptr, read_done = nullptr;
 };
 
 // Grow-only device buffer.
@@ -95,6 +103,9 @@ struct TuneState {
 struct rf_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // Copy streams of the asynchronous uploads and read-backs (lazily made).
+    cudaStream_t up = nullptr, down = nullptr;
+    std::vector<Mesh *> async_meshes;  // async meshes of the frame being built
     int nsm = 1;
     int device = 0;
     uint32_t tile_w = 32, warps = 4;
@@ -166,6 +177,63 @@ rf_status ensure(rf_ctx *ctx, DevBuf &b, size_t bytes) {
     }
     CK(cudaMalloc(&b.p, cap));
     b.cap = cap;
+    return RF_OK;
+}
+
+rf_status copy_streams(rf_ctx *ctx) {
+    if (!ctx->up) CK(cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking));
+    if (!ctx->down) CK(cudaStreamCreateWithFlags(&ctx->down, cudaStreamNonBlocking));
+    return RF_OK;
+}
+
+// First asynchronous use of a mesh / target: its events, and a `used` /
+// `rendered` mark covering every render queued so far.
+rf_status make_async(rf_ctx *ctx, Mesh &m) {
+    if (m.async) return RF_OK;
+    CK(cudaEventCreateWithFlags(&m.used, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&m.ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(m.used, ctx->stream));
+    m.async = true;
+    return RF_OK;
+}
+rf_status make_async(rf_ctx *ctx, Target &t) {
+    if (t.async) return RF_OK;
+    CK(cudaEventCreateWithFlags(&t.rendered, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&t.read_done, cudaEventDisableTiming));
+    CK(cudaEventRecord(t.rendered, ctx->stream));
+    t.async = true;
+    return RF_OK;
+}
+void drop_async(Mesh &m) {
+    if (m.used) cudaEventDestroy(m.used);
+    if (m.ready) cudaEventDestroy(m.ready);
+    m.used = m.ready = nullptr;
+}
+void drop_async(Target &t) {
+    if (t.rendered) cudaEventDestroy(t.rendered);
+    if (t.read_done) cudaEventDestroy(t.read_done);
+    t.rendered = t.read_done = nullptr;
+}
+// Work on the render stream that reads a mesh waits for its upload; work
+// that writes a target waits for its read-back.
+rf_status before_use(rf_ctx *ctx, Mesh &m) {
+    if (m.ready_pending) {
+        CK(cudaStreamWaitEvent(ctx->stream, m.ready, 0));
+        m.ready_pending = false;
+    }
+    return RF_OK;
+}
+rf_status before_write(rf_ctx *ctx, Target &t) {
+    if (t.read_pending) {
+        CK(cudaStreamWaitEvent(ctx->stream, t.read_done, 0));
+        t.read_pending = false;
+    }
+    return RF_OK;
+}
+rf_status sync_all(rf_ctx *ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->up) CK(cudaStreamSynchronize(ctx->up));
+    if (ctx->down) CK(cudaStreamSynchronize(ctx->down));
     return RF_OK;
 }
 
@@ -278,6 +346,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
     auto &hj = ctx->hjobs;
     hd.clear();
     hj.clear();
+    ctx->async_meshes.clear();
     host.assign(nin, JobHost{});
     uint64_t nv = 0, nt = 0;
     uint64_t tiles = 0, mask_words = 0;
@@ -291,7 +360,9 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
             const rf_draw &dr = ji.draws[i];
             auto mit = ctx->meshes.find(dr.mesh);
             if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
-            const Mesh &m = mit->second;
+            Mesh &m = mit->second;
+            if (m.async && (ctx->async_meshes.empty() || ctx->async_meshes.back() != &m))
+                ctx->async_meshes.push_back(&m);
             if (dr.shader < RF_SHADER_FLAT || dr.shader > RF_SHADER_GOURAUD_SRGB) return RF_ERR_BAD_ARG;
             if (m.nattr != nattr_for(dr.shader)) return RF_ERR_BAD_ARG;
             DrawDev d{};
@@ -516,6 +587,16 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     for (const JobDev &J : hj)
         fast = fast && J.depth && J.depth_test == RF_DEPTH_LESS && J.color_write && J.depth_write;
 
+    // Asynchronous uploads of the meshes read and read-backs of the targets
+    // written must finish first.
+    std::sort(ctx->async_meshes.begin(), ctx->async_meshes.end());
+    ctx->async_meshes.erase(std::unique(ctx->async_meshes.begin(), ctx->async_meshes.end()),
+                            ctx->async_meshes.end());
+    for (Mesh *m : ctx->async_meshes)
+        if ((st = before_use(ctx, *m))) return st;
+    for (uint32_t k = 0; k < nin; ++k)
+        if (host[k].slot >= 0 && (st = before_write(ctx, *in[k].tg))) return st;
+
     // Per-frame parameters travel as data (draws, jobs); the launch sequence
     // below depends only on the sizes, so it is replayed as a CUDA graph when
     // a frame of the same shape comes again.
@@ -629,13 +710,19 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if (ctx->timing) ctx->ev_pending.push_back(ev);
     for (uint32_t k = 0; k < nin; ++k)
         if (host[k].slot >= 0) in[k].tg->clear_flags = 0;  // the raster pass wrote the pending clear
+    for (Mesh *m : ctx->async_meshes) CK(cudaEventRecord(m->used, s));
+    for (uint32_t k = 0; k < nin; ++k)
+        if (host[k].slot >= 0 && in[k].tg->async) CK(cudaEventRecord(in[k].tg->rendered, s));
     return RF_OK;
 }
 
 rf_status flush_clear(rf_ctx *ctx, Target &tg) {
     if (!tg.clear_flags) return RF_OK;
+    rf_status st = before_write(ctx, tg);
+    if (st) return st;
     CK(rfk::launch_fill(tg.color, tg.depth, (size_t)tg.w * tg.h, tg.clear_px, tg.clear_z,
                         tg.clear_flags, ctx->nsm, ctx->stream));
+    if (tg.async) CK(cudaEventRecord(tg.rendered, ctx->stream));
     ctx->kernels += 1;
     tg.clear_flags = 0;
     return RF_OK;
@@ -702,10 +789,12 @@ rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out) {
 
 rf_status rf_ctx_destroy(rf_ctx *ctx) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    cudaStreamSynchronize(ctx->stream);
-    for (auto &kv : ctx->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); }
+    sync_all(ctx);
+    for (auto &kv : ctx->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); drop_async(kv.second); }
     for (auto &kv : ctx->textures) cudaFree(kv.second.texels);
-    for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); }
+    for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); drop_async(kv.second); }
+    if (ctx->up) cudaStreamDestroy(ctx->up);
+    if (ctx->down) cudaStreamDestroy(ctx->down);
     graphs_drop(ctx);
     for (TuneState &t : ctx->tunes) {
         if (t.e0) cudaEventDestroy(t.e0);
@@ -734,8 +823,7 @@ rf_status rf_ctx_device(rf_ctx *ctx, int32_t *device) {
 
 rf_status rf_ctx_sync(rf_ctx *ctx) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    CK(cudaStreamSynchronize(ctx->stream));
-    return RF_OK;
+    return sync_all(ctx);
 }
 
 rf_status rf_ctx_take_stats(rf_ctx *ctx, rf_stats *out) {
@@ -833,9 +921,33 @@ rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const ui
         for (uint64_t i = 0; i < 3ull * m.ntri; ++i)
             if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
     const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * 12;
+    rf_status st = before_use(ctx, m);  // an asynchronous upload still in flight
+    if (st) return st;
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (verts) mesh_bbox(m, verts);
+    return RF_OK;
+}
+
+rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->meshes.find(mesh);
+    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    Mesh &m = it->second;
+    if (idx)
+        for (uint64_t i = 0; i < 3ull * m.ntri; ++i)
+            if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
+    rf_status st = copy_streams(ctx);
+    if (st) return st;
+    if ((st = make_async(ctx, m))) return st;
+    const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * 12;
+    // The copy waits for every queued render that reads the mesh.
+    CK(cudaStreamWaitEvent(ctx->up, m.used, 0));
+    if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->up));
+    if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->up));
+    CK(cudaEventRecord(m.ready, ctx->up));
+    m.ready_pending = true;
     if (verts) mesh_bbox(m, verts);
     return RF_OK;
 }
@@ -854,9 +966,11 @@ rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh) {
     if (!ctx) return RF_ERR_BAD_ARG;
     auto it = ctx->meshes.find(mesh);
     if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
-    CK(cudaStreamSynchronize(ctx->stream));
+    rf_status st = sync_all(ctx);
+    if (st) return st;
     cudaFree(it->second.verts);
     cudaFree(it->second.idx);
+    drop_async(it->second);
     ctx->meshes.erase(it);
     return RF_OK;
 }
@@ -912,9 +1026,11 @@ rf_status rf_target_destroy(rf_ctx *ctx, rf_target t) {
     if (!ctx) return RF_ERR_BAD_ARG;
     auto it = ctx->targets.find(t);
     if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
-    CK(cudaStreamSynchronize(ctx->stream));
+    rf_status st = sync_all(ctx);
+    if (st) return st;
     cudaFree(it->second.color);
     cudaFree(it->second.depth);
+    drop_async(it->second);
     ctx->targets.erase(it);
     return RF_OK;
 }
@@ -944,6 +1060,7 @@ rf_status rf_target_write(rf_ctx *ctx, rf_target t, const uint32_t *color, const
     Target &tg = it->second;
     rf_status st = flush_clear(ctx, tg);
     if (st) return st;
+    if ((st = before_write(ctx, tg))) return st;
     const size_t n = (size_t)tg.w * tg.h * 4;
     if (color) CK(cudaMemcpyAsync(tg.color, color, n, cudaMemcpyHostToDevice, ctx->stream));
     if (depth && tg.depth) CK(cudaMemcpyAsync(tg.depth, depth, n, cudaMemcpyHostToDevice, ctx->stream));
@@ -962,6 +1079,25 @@ rf_status rf_target_read(rf_ctx *ctx, rf_target t, uint32_t *color, float *depth
     if (color) CK(cudaMemcpyAsync(color, tg.color, n, cudaMemcpyDeviceToHost, ctx->stream));
     if (depth && tg.depth) CK(cudaMemcpyAsync(depth, tg.depth, n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return RF_OK;
+}
+
+rf_status rf_target_read_async(rf_ctx *ctx, rf_target t, uint32_t *color, float *depth) {
+    if (!ctx) return RF_ERR_BAD_ARG;
+    auto it = ctx->targets.find(t);
+    if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    Target &tg = it->second;
+    rf_status st = copy_streams(ctx);
+    if (st) return st;
+    if ((st = make_async(ctx, tg))) return st;
+    if ((st = flush_clear(ctx, tg))) return st;
+    const size_t n = (size_t)tg.w * tg.h * 4;
+    // The copy waits for every queued render into the target.
+    CK(cudaStreamWaitEvent(ctx->down, tg.rendered, 0));
+    if (color) CK(cudaMemcpyAsync(color, tg.color, n, cudaMemcpyDeviceToHost, ctx->down));
+    if (depth && tg.depth) CK(cudaMemcpyAsync(depth, tg.depth, n, cudaMemcpyDeviceToHost, ctx->down));
+    CK(cudaEventRecord(tg.read_done, ctx->down));
+    tg.read_pending = true;
     return RF_OK;
 }
 
