@@ -210,6 +210,20 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
                           const float viewport[16], rf_target target,
                           const rf_context_flags *flags, rf_stats *stats);
 
+/* ---- line primitives ---------------------------------------------------
+ * One render() call of Edge<usize> primitives (prim.rs:41-60): a line mesh
+ * holds nlines vertex index pairs.  Lines are clipped like clip.rs:311-348,
+ * never back-facing (face_cull FRONT drops them all, ctx.rs:95-101), drawn
+ * one pixel per column or row by line() (raster.rs:115-173) with the first
+ * vertex's depth and varyings, and counted like render() (render.rs:
+ * 150-206).  A line longer than 2^22 pixels counts once in oob and is not
+ * drawn.  Line meshes are rejected by the triangle entry points. */
+rf_status rf_lines_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
+                          uint32_t nattr, const uint32_t *idx, uint32_t nlines, rf_mesh *out);
+rf_status rf_render_lines(rf_ctx *ctx, rf_mesh lines, int32_t shader, const rf_uniforms *uniforms,
+                          const float viewport[16], rf_target target, const rf_context_flags *flags,
+                          rf_stats *stats);
+
 /* ---- batched scenes ----------------------------------------------------
  * A scene = one target and the render() calls that draw into it, in order
  * (a frame of demos/src/bin/crates.rs:114-133).  rf_render_batch renders

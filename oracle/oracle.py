@@ -59,6 +59,10 @@ def lib():
         L.rfo_tri_fill.restype = C.c_uint32
         L.rfo_sample.argtypes = [u32p, C.c_uint32, C.c_uint32, C.c_int32, C.c_float, C.c_float]
         L.rfo_sample.restype = C.c_uint32
+        L.rfo_render_lines.argtypes = [C.POINTER(Draw), u32p, C.c_uint32, fp, u32p, fp,
+                                       C.c_uint32, C.c_uint32, C.c_int32, C.POINTER(Ctx),
+                                       C.POINTER(Stats)]
+        L.rfo_render_lines.restype = None
         L.rfo_bbox_status.argtypes = [fp, C.c_uint32, C.c_uint32, fp]
         L.rfo_bbox_status.restype = C.c_int32
         _lib = L
@@ -169,3 +173,21 @@ def bbox_status(verts, mvp, pos_dim=3):
     v = np.ascontiguousarray(verts, np.float32)
     m = np.ascontiguousarray(mvp, np.float32).reshape(-1)
     return int(lib().rfo_bbox_status(_fp(v), v.shape[0], v.shape[1], _fp(m)))
+
+
+def render_lines(verts, lines, shader, viewport, color, depth, ctx, mvp=None, pos_dim=3,
+                 flat_rgba=0, tex=None, sampler=0, pixfmt=0, stats=None):
+    """One render() call of Edge<usize> primitives: `lines` (n, 2) vertex
+    index pairs (raster.rs line(), clip.rs line clipping)."""
+    L = lib()
+    h, w = color.shape
+    d = make_draw(verts, np.zeros((0, 3), np.uint32), shader, mvp, pos_dim, flat_rgba, tex, sampler)
+    li = np.ascontiguousarray(lines, np.uint32).reshape(-1)
+    vp = np.ascontiguousarray(viewport, np.float32).reshape(-1)
+    st = stats if stats is not None else Stats()
+    c = Ctx(ctx.get("depth_test", 1), int(ctx.get("color_write", True)),
+            int(ctx.get("depth_write", True)), ctx.get("face_cull", 1))
+    dp = _fp(depth) if depth is not None else C.POINTER(C.c_float)()
+    L.rfo_render_lines(C.byref(d), _u32p(li), li.size // 2, _fp(vp), _u32p(color), dp, w, h,
+                       pixfmt, C.byref(c), C.byref(st))
+    return st

@@ -12,6 +12,7 @@
 #include "rf_oracle.h"
 
 #include <cmath>
+#include <utility>
 #include <cstring>
 
 namespace {
@@ -522,6 +523,156 @@ extern "C" void rfo_render(const rfo_draw *d, const float vp[16], uint32_t *colo
             render_t<5, RFO_TEX_GOURAUD>(d, vp, color, depth, w, h, fmt, ctx, st);
             break;
         default: render_t<3, RFO_GOURAUD_SRGB>(d, vp, color, depth, w, h, fmt, ctx, st); break;
+    }
+}
+
+// render.rs:134-207 for Edge<usize> (prim.rs:41-60): vertex shader,
+// line clipping (clip.rs:311-348), to_screen (prim.rs:62-88),
+// face_cull(is_backface = false: render.rs:92-94 default) and line()
+// (raster.rs:115-173); every pixel is a one-pixel scanline into
+// rasterize_fb (target.rs:163-198) carrying the first vertex's position and
+// varyings.  idx holds nlines index pairs.
+// Lines longer than this many pixels along their stepping axis (far past
+// any target; the reference would index out of bounds) count once in oob.
+constexpr uint64_t LINE_MAX_SPAN = 4194304u;
+
+template <int NA, int S>
+void render_lines_t(const rfo_draw *d, const uint32_t *idx, uint32_t nlines, const float vp[16],
+                    uint32_t *color, float *depth, uint32_t w, uint32_t h, int32_t fmt,
+                    const rfo_ctx *ctx, rfo_stats *st) {
+    constexpr uint32_t ZM = zdiv_mask<S>();
+    st->calls += 1;
+    st->prims_i += nlines;
+    st->verts_i += d->nverts;
+    const uint32_t stride = d->pos_dim + d->nattr;
+    ClipVert<NA> *cv = new ClipVert<NA>[d->nverts > 0 ? d->nverts : 1];
+    for (uint32_t i = 0; i < d->nverts; ++i) {
+        const float *src = d->verts + (uint64_t)i * stride;
+        if (d->pos_dim == 4) {
+            for (int k = 0; k < 4; ++k) cv[i].pos[k] = src[k];
+        } else {
+            const float hom[4] = {src[0], src[1], src[2], 1.0f};
+            for (int k = 0; k < 4; ++k) cv[i].pos[k] = dot4(d->mvp + 4 * k, hom);
+        }
+        for (int k = 0; k < NA; ++k) cv[i].a[k] = src[d->pos_dim + k];
+        cv[i].oc = outcode(cv[i].pos);
+    }
+    // One pixel of a line: the one-pixel scanline {y, x..x+1} with the
+    // line's first-vertex varyings v (target.rs:163-198; a row below the
+    // buffer counts in oob only, a pixel past the right edge keeps frags.i
+    // and counts in oob, as for triangle spans).
+    auto pixel = [&](uint64_t x, uint64_t y, const Var<NA> &v) {
+        if (y >= h) {
+            st->oob += 1;
+            return;
+        }
+        st->frags_i += 1;
+        if (x >= w) {
+            st->oob += 1;
+            return;
+        }
+        Var<NA> f = v;
+        for (int a = 0; a < NA; ++a)
+            if ((ZM >> a) & 1) f.a[a] = v.a[a] / v.p[2];
+        const float new_z = v.p[2];
+        const uint64_t i = y * (uint64_t)w + x;
+        bool pass = true;
+        if (depth) {
+            const float cur = depth[i];
+            switch (ctx->depth_test) {
+                case RFO_DEPTH_NONE: pass = true; break;
+                case RFO_DEPTH_LESS: pass = cur < new_z; break;
+                case RFO_DEPTH_EQUAL: pass = cur == new_z; break;
+                default: pass = cur > new_z; break;
+            }
+        }
+        if (pass) {
+            const uint32_t col = shade<NA, S>(d, f);
+            if (ctx->color_write) {
+                st->frags_o += 1;
+                color[i] = rfo_pack(col, fmt);
+            }
+            if (depth && ctx->depth_write) depth[i] = new_z;
+        }
+    };
+    for (uint32_t l = 0; l < nlines; ++l) {
+        ClipVert<NA> a = cv[idx[2 * l]], b = cv[idx[2 * l + 1]];
+        if (a.oc & b.oc) continue;  // both outside one plane
+        if (a.oc | b.oc) {
+            bool drop = false;
+            for (int p = 0; p < 6 && !drop; ++p) {
+                const bool a_in = (a.oc & (1u << p)) == 0, b_in = (b.oc & (1u << p)) == 0;
+                if (!a_in && !b_in) {
+                    drop = true;
+                    break;
+                }
+                ClipVert<NA> v;
+                if (intersect<NA>(p, a, b, v)) {
+                    if (a_in) b = v;
+                    else if (b_in) a = v;
+                }
+            }
+            if (drop) continue;
+        }
+        Var<NA> sv[2];
+        const ClipVert<NA> *e[2] = {&a, &b};
+        for (int k = 0; k < 2; ++k) {
+            const ClipVert<NA> &v = *e[k];
+            const float wv = v.pos[3];
+            const float ndc[4] = {v.pos[0] / wv, v.pos[1] / wv, 1.0f / wv, 1.0f};
+            sv[k].p[0] = dot4(vp + 0, ndc);
+            sv[k].p[1] = dot4(vp + 4, ndc);
+            sv[k].p[2] = dot4(vp + 8, ndc);
+            for (int q = 0; q < NA; ++q) sv[k].a[q] = ((ZM >> q) & 1) ? v.a[q] / wv : v.a[q];
+        }
+        if (ctx->face_cull == RFO_CULL_FRONT) continue;  // face_cull(false)
+        st->prims_o += 1;
+        st->verts_o += 3;
+        // raster.rs:121-173 line().
+        Var<NA> v0 = sv[0], v1 = sv[1];
+        if (v0.p[1] > v1.p[1]) std::swap(v0, v1);
+        const float dx = v1.p[0] - v0.p[0], dy = v1.p[1] - v0.p[1];
+        if (std::fabs(dx) > dy) {
+            if (dx < 0.0f) std::swap(v0, v1);  // dx, dy keep their values
+            const float x0 = round_up_to_half(v0.p[0]), x1 = round_up_to_half(v1.p[0]);
+            const float dy_dx = dy / dx;
+            float y = v0.p[1] + dy_dx * (x0 - v0.p[0]);
+            if (as_usize(x1) > as_usize(x0) && as_usize(x1) - as_usize(x0) > LINE_MAX_SPAN) {
+                st->oob += 1;  // out of the supported range: counted, not drawn
+                continue;
+            }
+            for (uint64_t x = as_usize(x0), xe = as_usize(x1); x < xe; ++x) {
+                pixel(x, as_usize(y), v0);
+                y = y + dy_dx;
+            }
+        } else {
+            const float y0 = round_up_to_half(v0.p[1]), y1 = round_up_to_half(v1.p[1]);
+            const float dx_dy = dx / dy;
+            float x = v0.p[0] + dx_dy * (y0 - v0.p[1]);
+            if (as_usize(y1) > as_usize(y0) && as_usize(y1) - as_usize(y0) > LINE_MAX_SPAN) {
+                st->oob += 1;
+                continue;
+            }
+            for (uint64_t y = as_usize(y0), ye = as_usize(y1); y < ye; ++y) {
+                pixel(as_usize(x), y, v0);
+                x = x + dx_dy;
+            }
+        }
+    }
+    delete[] cv;
+}
+
+extern "C" void rfo_render_lines(const rfo_draw *d, const uint32_t *idx, uint32_t nlines,
+                                 const float vp[16], uint32_t *color, float *depth, uint32_t w,
+                                 uint32_t h, int32_t fmt, const rfo_ctx *ctx, rfo_stats *st) {
+    switch (d->shader) {
+        case RFO_FLAT: render_lines_t<0, RFO_FLAT>(d, idx, nlines, vp, color, depth, w, h, fmt, ctx, st); break;
+        case RFO_GOURAUD: render_lines_t<3, RFO_GOURAUD>(d, idx, nlines, vp, color, depth, w, h, fmt, ctx, st); break;
+        case RFO_TEXTURED: render_lines_t<2, RFO_TEXTURED>(d, idx, nlines, vp, color, depth, w, h, fmt, ctx, st); break;
+        case RFO_TEX_GOURAUD:
+            render_lines_t<5, RFO_TEX_GOURAUD>(d, idx, nlines, vp, color, depth, w, h, fmt, ctx, st);
+            break;
+        default: render_lines_t<3, RFO_GOURAUD_SRGB>(d, idx, nlines, vp, color, depth, w, h, fmt, ctx, st); break;
     }
 }
 

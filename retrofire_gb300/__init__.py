@@ -128,6 +128,10 @@ _SIGS = {
     "rf_render_draws": [_P, C.POINTER(Draw), C.c_uint32, C.POINTER(C.c_float), C.c_uint64,
                         C.POINTER(Flags), C.POINTER(CStats)],
     "rf_render_batch": [_P, C.POINTER(Job), C.c_uint32, C.POINTER(CStats)],
+    "rf_lines_upload": [_P, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_uint32,
+                        C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint64)],
+    "rf_render_lines": [_P, C.c_uint64, C.c_int32, C.POINTER(Uniforms), C.POINTER(C.c_float),
+                        C.c_uint64, C.POINTER(Flags), C.POINTER(CStats)],
     "rf_ctx_device": [_P, C.POINTER(C.c_int32)],
     "rf_mesh_info": [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                      C.POINTER(C.c_uint32)],
@@ -343,6 +347,36 @@ class Mesh:
         if self.handle and self.dev.ptr:
             lib().rf_mesh_destroy(self.dev.ptr, self.handle)
         self.handle = 0
+
+
+class Lines(Mesh):
+    """A device line mesh: verts as for Mesh, lines (n, 2) vertex index
+    pairs (Edge<usize>, geom/prim.rs)."""
+
+    def __init__(self, verts, lines, pos_dim=3, device=None):
+        self.dev = device or default_device()
+        v = np.ascontiguousarray(verts, np.float32)
+        li = np.ascontiguousarray(lines, np.uint32).reshape(-1)
+        self.nverts, self.ntri = v.shape[0], li.size // 2
+        self.pos_dim, self.nattr = pos_dim, v.shape[1] - pos_dim
+        h = C.c_uint64()
+        _check(lib().rf_lines_upload(self.dev.ptr, _fp(v), v.shape[0], pos_dim, self.nattr,
+                                     _u32p(li), self.ntri, C.byref(h)), "rf_lines_upload")
+        self.handle = h.value
+
+
+def render_lines(lines, shader, uniform, to_screen, target, ctx=None):
+    """render() of line primitives (Edge<usize>): lines is a Lines mesh."""
+    ctx = ctx or Context()
+    vp = np.ascontiguousarray(to_screen, np.float32).reshape(-1)
+    u = shader.uniforms(uniform)
+    fl = ctx.flags()
+    cs = CStats()
+    _check(lib().rf_render_lines(target.dev.ptr, lines.handle, shader.kind, C.byref(u), _fp(vp),
+                                 target.handle, C.byref(fl), C.byref(cs)), "rf_render_lines")
+    st = Stats.from_c(cs)
+    ctx.stats += st
+    return st
 
 
 class Texture:

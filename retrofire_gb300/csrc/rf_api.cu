@@ -24,7 +24,8 @@ namespace {
 struct Mesh {
     float *verts = nullptr;
     uint32_t *idx = nullptr;
-    uint32_t nverts = 0, ntri = 0, pos_dim = 3, nattr = 0;
+    uint32_t nverts = 0, ntri = 0, pos_dim = 3, nattr = 0;  // ntri: lines of a line mesh
+    bool lines = false;  // Edge<usize> primitives (index pairs), rf_render_lines
     // BBox::of the positions (render/scene.rs:37-39): low x,y,z, high x,y,z
     float bbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
     // Asynchronous updates (rf_mesh_update_async): `used` marks the last
@@ -116,6 +117,7 @@ struct rf_ctx {
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
     DevBuf triw, trib, scan64, rowtot, rows, rprims, jstats;
+    DevBuf lrec, lmask;  // line pass
     // CUDA graphs of the launch sequence, keyed by frame shape (graph mode).
     bool graphs = false;
     uint64_t gen = 0;  // bumped whenever a scratch buffer moves
@@ -361,6 +363,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
             auto mit = ctx->meshes.find(dr.mesh);
             if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
             Mesh &m = mit->second;
+            if (m.lines) return RF_ERR_BAD_ARG;  // line meshes render with rf_render_lines
             if (m.async && (ctx->async_meshes.empty() || ctx->async_meshes.back() != &m))
                 ctx->async_meshes.push_back(&m);
             if (dr.shader < RF_SHADER_FLAT || dr.shader > RF_SHADER_GOURAUD_SRGB) return RF_ERR_BAD_ARG;
@@ -803,7 +806,7 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
-                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->jstats};
+                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->jstats, &ctx->lrec, &ctx->lmask};
     if (ctx->rows_need_host) cudaFreeHost(ctx->rows_need_host);
     if (ctx->rows_evt) cudaEventDestroy(ctx->rows_evt);
     for (DevBuf *b : bufs) cudaFree(b->p);
@@ -912,15 +915,127 @@ rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint3
     return RF_OK;
 }
 
+rf_status rf_lines_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
+                          uint32_t nattr, const uint32_t *idx, uint32_t nlines, rf_mesh *out) {
+    if (!ctx || !out || (pos_dim != 3 && pos_dim != 4) || nattr > RF_MAX_ATTR) return RF_ERR_BAD_ARG;
+    if ((nverts && !verts) || (nlines && !idx)) return RF_ERR_BAD_ARG;
+    for (uint64_t i = 0; i < 2ull * nlines; ++i)
+        if (idx[i] >= nverts) return RF_ERR_BAD_ARG;  // `vs[i]` would panic (prim.rs:53-55)
+    Mesh m;
+    m.nverts = nverts;
+    m.ntri = nlines;
+    m.pos_dim = pos_dim;
+    m.nattr = nattr;
+    m.lines = true;
+    const size_t vb = (size_t)nverts * (pos_dim + nattr) * 4, ib = (size_t)nlines * 8;
+    if (vb) CK(cudaMalloc(&m.verts, vb));
+    if (ib) CK(cudaMalloc(&m.idx, ib));
+    if (vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
+    if (ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    mesh_bbox(m, verts);
+    const uint64_t h = ctx->next_handle++;
+    ctx->meshes[h] = m;
+    *out = h;
+    return RF_OK;
+}
+
+rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_uniforms *u,
+                          const float viewport[16], rf_target target, const rf_context_flags *fl,
+                          rf_stats *stats) {
+    if (!ctx || !u || !viewport || !flags_ok(fl)) return RF_ERR_BAD_ARG;
+    auto mit = ctx->meshes.find(mesh);
+    if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    auto tit = ctx->targets.find(target);
+    if (tit == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+    Mesh &m = mit->second;
+    Target &tg = tit->second;
+    if (!m.lines) return RF_ERR_BAD_ARG;
+    if (shader < RF_SHADER_FLAT || shader > RF_SHADER_GOURAUD_SRGB || m.nattr != nattr_for(shader))
+        return RF_ERR_BAD_ARG;
+    rf_status st = init_stats(ctx);
+    if (st) return st;
+    DrawDev d{};
+    d.verts = m.verts;
+    d.idx = m.idx;
+    d.nverts = m.nverts;
+    d.ntri = m.ntri;
+    d.pos_dim = m.pos_dim;
+    d.nattr = m.nattr;
+    d.stride = m.pos_dim + m.nattr;
+    d.shader = shader;
+    d.sampler = (int32_t)u->sampler;
+    d.flat_rgba = u->flat_rgba;
+    if (shader == RF_SHADER_TEXTURED || shader == RF_SHADER_TEX_GOURAUD) {
+        auto xit = ctx->textures.find(u->texture);
+        if (xit == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+        if (d.sampler < RF_SAMPLER_REPEAT_POT || d.sampler > RF_SAMPLER_ONCE) return RF_ERR_BAD_ARG;
+        if (d.sampler == RF_SAMPLER_REPEAT_POT && (!is_pot(xit->second.w) || !is_pot(xit->second.h)))
+            return RF_ERR_NON_POT_TEXTURE;
+        d.tex = xit->second.texels;
+        d.tw = xit->second.w;
+        d.th = xit->second.h;
+    }
+    memcpy(d.mvp, u->mvp, sizeof d.mvp);
+    ctx->host_acc.calls += 1;  // render.rs:152-155
+    ctx->host_acc.prims_i += m.ntri;
+    ctx->host_acc.verts_i += m.nverts;
+    if (m.ntri && m.nverts) {
+        // The line pass writes the target directly: a pending clear first.
+        if ((st = flush_clear(ctx, tg))) return st;
+        if ((st = before_use(ctx, m))) return st;
+        if ((st = before_write(ctx, tg))) return st;
+        JobDev J{};
+        J.color = tg.color;
+        J.depth = tg.depth;
+        J.w = tg.w;
+        J.h = tg.h;
+        J.pixfmt = tg.fmt;
+        J.depth_test = fl->depth_test;
+        J.color_write = fl->color_write;
+        J.depth_write = fl->depth_write;
+        J.face_cull = fl->face_cull;
+        J.tiles_x = (tg.w + RF_TILE_H - 1) / RF_TILE_H;
+        J.tiles_y = (tg.h + RF_TILE_H - 1) / RF_TILE_H;
+        J.ntri = m.ntri;
+        J.mask_words = (m.ntri + 31) / 32;
+        memcpy(J.vp, viewport, sizeof J.vp);
+        const uint32_t ntiles = J.tiles_x * J.tiles_y;
+        const size_t mwords = (size_t)ntiles * J.mask_words;
+        if ((st = ensure(ctx, ctx->draws, sizeof(DrawDev)))) return st;
+        if ((st = ensure(ctx, ctx->jobs, sizeof(JobDev)))) return st;
+        if ((st = ensure(ctx, ctx->cpos, (size_t)m.nverts * sizeof(float4)))) return st;
+        if ((st = ensure(ctx, ctx->coc, m.nverts))) return st;
+        if ((st = ensure(ctx, ctx->lrec, (size_t)m.ntri * sizeof(LineRec)))) return st;
+        if ((st = ensure(ctx, ctx->lmask, mwords * 4))) return st;
+        cudaStream_t s = ctx->stream;
+        CK(cudaMemcpyAsync(ctx->draws.p, &d, sizeof d, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->jobs.p, &J, sizeof J, cudaMemcpyHostToDevice, s));
+        uint32_t *counters = P<uint32_t>(ctx->counters);
+        CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
+        CK(cudaMemsetAsync(ctx->lmask.p, 0, mwords * 4, s));
+        CK(rfk::launch_vertex(P<DrawDev>(ctx->draws), 1, m.nverts, P<float4>(ctx->cpos),
+                              P<uint8_t>(ctx->coc), ctx->nsm, s));
+        CK(rfk::launch_lines(P<DrawDev>(ctx->draws), P<JobDev>(ctx->jobs), m.ntri, P<float4>(ctx->cpos),
+                             P<uint8_t>(ctx->coc), P<LineRec>(ctx->lrec), P<uint32_t>(ctx->lmask), ntiles,
+                             counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->nsm, s));
+        ctx->kernels += 3;
+        if (m.async) CK(cudaEventRecord(m.used, s));
+        if (tg.async) CK(cudaEventRecord(tg.rendered, s));
+    }
+    return finish_call(ctx, stats);
+}
+
 rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx) {
     if (!ctx) return RF_ERR_BAD_ARG;
     auto it = ctx->meshes.find(mesh);
     if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = it->second;
+    const uint32_t per = m.lines ? 2u : 3u;
     if (idx)
-        for (uint64_t i = 0; i < 3ull * m.ntri; ++i)
+        for (uint64_t i = 0; i < (uint64_t)per * m.ntri; ++i)
             if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
-    const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * 12;
+    const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * per * 4;
     rf_status st = before_use(ctx, m);  // an asynchronous upload still in flight
     if (st) return st;
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
@@ -935,13 +1050,14 @@ rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, co
     auto it = ctx->meshes.find(mesh);
     if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = it->second;
+    const uint32_t per = m.lines ? 2u : 3u;
     if (idx)
-        for (uint64_t i = 0; i < 3ull * m.ntri; ++i)
+        for (uint64_t i = 0; i < (uint64_t)per * m.ntri; ++i)
             if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
     rf_status st = copy_streams(ctx);
     if (st) return st;
     if ((st = make_async(ctx, m))) return st;
-    const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * 12;
+    const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * per * 4;
     // The copy waits for every queued render that reads the mesh.
     CK(cudaStreamWaitEvent(ctx->up, m.used, 0));
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->up));

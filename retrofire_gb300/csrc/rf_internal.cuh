@@ -129,4 +129,18 @@ struct RasterPrim {
     uint32_t pad_[3];
 };
 
+// One line after clipping and to_screen (raster.rs:121-173): it steps
+// along x (wide) or y, n pixels from `begin`; the other coordinate of
+// pixel k is the k-step running sum s0 + d + ... (as usize); every pixel has
+// depth z and the packed colour of the line's fragment.
+#define RF_LINE_MAX_SPAN 4194304u  // longer lines (2^22 px) count in oob, not drawn
+struct LineRec {
+    uint32_t live, wide;
+    uint64_t begin;
+    uint32_t n;
+    float s0, d, z;
+    uint32_t color;
+    uint32_t pad_;
+};
+
 #endif

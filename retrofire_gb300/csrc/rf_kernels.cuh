@@ -94,6 +94,11 @@ cudaError_t launch_fill(uint32_t *color, float *depth, size_t n, uint32_t px, fl
 // Object culling of the draws with RF_DRAW_CULL_BBOX (sets DrawDev::culled
 // and counts into stats[draw.job]).
 cudaError_t launch_cull(DrawDev *draws, uint32_t nd, StatsDev *stats, int nsm, cudaStream_t s);
+// Line primitives (rf_lines.cu): setup + tile raster of one line draw
+// (draws[0], jobs[0]; mask zeroed, queue zeroed).
+cudaError_t launch_lines(const DrawDev *draws, const JobDev *jobs, uint32_t nl, const float4 *cpos,
+                         const uint8_t *coc, LineRec *recs, uint32_t *mask, uint32_t ntiles,
+                         uint32_t *queue, StatsDev *stats, int nsm, cudaStream_t s);
 // Adds the n per-job stats slots js[0..n) into *total (one block).
 cudaError_t launch_stats_fold(const StatsDev *js, uint32_t n, StatsDev *total, cudaStream_t s);
 }  // namespace rfk
