@@ -311,3 +311,18 @@ def test_bad_arguments():
     for o in (m, tex, tg):
         o.close()
     dev.close()
+
+
+def test_text_mesh_renders_like_the_oracle():
+    """A text mesh (text.rs: quads from an atlas) through the textured path
+    with the clamp sampler."""
+    from retrofire_gb300 import text
+    atl = text.Atlas(scenes.noise_texture(128, 5)[:64], 8, 8)
+    t = text.Text(atl)
+    t.write("retrofire on\na GB300 !")
+    v, f = t.mesh()
+    mvp = np.array([[1 / 64, 0, 0, -1], [0, -1 / 32, 0, 1], [0, 0, 0, 0.5], [0, 0, 0, 1]], np.float32)
+    d = DrawSpec(v, f, rf.TEXTURED, mvp, tex=atl.texels, sampler=rf.CLAMP)
+    g, o = both([d], mat.viewport(0, 0, 256, 128), 256, 128, ctx=rf.Context(face_cull=rf.CULL_NONE))
+    assert o[2]["frags_o"] > 1000
+    assert_parity(g, o)
