@@ -67,6 +67,11 @@ struct rf_server {
     // Worker-only state: free targets by (w, h, format, depth).
     std::unordered_map<uint64_t, std::vector<rf_target>> pool;
     uint64_t pool_bytes = 0;  // all pooled targets, free or in use
+    // Page-locked staging of a batch's images (grow-only): the read-backs
+    // run at page-locked speed, then the host copies into the callers'
+    // buffers.
+    char *stage = nullptr;
+    size_t stage_cap = 0;
 };
 
 namespace {
@@ -135,13 +140,64 @@ void serve(rf_server *S, std::vector<Req> &batch, uint64_t batch_id) {
         for (size_t k = 0; k < jobs.size(); ++k) res[of[k]].status = st;
     }
     const Clock::time_point t_gpu = Clock::now();
+    // Read-backs into the staging area, one wait, then host copies.
+    size_t need = 0;
+    std::vector<size_t> off(n, 0);
     for (size_t k = 0; k < jobs.size(); ++k) {
         const size_t i = of[k];
         if (res[i].status != RF_OK) continue;
-        res[i].stats = stats[k];
-        if (batch[i].color_out || (batch[i].depth_out && batch[i].has_depth))
-            res[i].status = rf_target_read(S->ctx, tg[i], batch[i].color_out,
-                                           batch[i].has_depth ? batch[i].depth_out : nullptr);
+        off[i] = need;
+        const size_t px = (size_t)batch[i].w * batch[i].h * 4;
+        if (batch[i].color_out) need += px;
+        if (batch[i].depth_out && batch[i].has_depth) need += px;
+    }
+    bool staged = false;
+    if (need > S->stage_cap) {
+        if (S->stage) cudaFreeHost(S->stage);
+        S->stage = nullptr;
+        S->stage_cap = 0;
+        const size_t cap = need + need / 2;
+        if (cudaHostAlloc(reinterpret_cast<void **>(&S->stage), cap, cudaHostAllocDefault) == cudaSuccess)
+            S->stage_cap = cap;
+        else
+            S->stage = nullptr;
+    }
+    if (S->stage && need <= S->stage_cap) {
+        staged = true;
+        for (size_t k = 0; k < jobs.size(); ++k) {
+            const size_t i = of[k];
+            if (res[i].status != RF_OK) continue;
+            res[i].stats = stats[k];
+            const size_t px = (size_t)batch[i].w * batch[i].h * 4;
+            uint32_t *c = batch[i].color_out ? reinterpret_cast<uint32_t *>(S->stage + off[i]) : nullptr;
+            float *d = (batch[i].depth_out && batch[i].has_depth)
+                           ? reinterpret_cast<float *>(S->stage + off[i] + (c ? px : 0))
+                           : nullptr;
+            if (c || d) res[i].status = rf_target_read_async(S->ctx, tg[i], c, d);
+        }
+        const rf_status ss = rf_ctx_sync(S->ctx);
+        for (size_t k = 0; k < jobs.size(); ++k) {
+            const size_t i = of[k];
+            if (res[i].status != RF_OK) continue;
+            if (ss != RF_OK) {
+                res[i].status = ss;
+                continue;
+            }
+            const size_t px = (size_t)batch[i].w * batch[i].h * 4;
+            if (batch[i].color_out) memcpy(batch[i].color_out, S->stage + off[i], px);
+            if (batch[i].depth_out && batch[i].has_depth)
+                memcpy(batch[i].depth_out, S->stage + off[i] + (batch[i].color_out ? px : 0), px);
+        }
+    }
+    if (!staged) {  // no page-locked memory to be had: direct reads
+        for (size_t k = 0; k < jobs.size(); ++k) {
+            const size_t i = of[k];
+            if (res[i].status != RF_OK) continue;
+            res[i].stats = stats[k];
+            if (batch[i].color_out || (batch[i].depth_out && batch[i].has_depth))
+                res[i].status = rf_target_read(S->ctx, tg[i], batch[i].color_out,
+                                               batch[i].has_depth ? batch[i].depth_out : nullptr);
+        }
     }
     const Clock::time_point t_done = Clock::now();
     for (size_t i = 0; i < n; ++i)
@@ -298,6 +354,7 @@ rf_status rf_server_destroy(rf_server *S) {
     cudaSetDevice(S->device);
     for (auto &kv : S->pool)
         for (rf_target t : kv.second) rf_target_destroy(S->ctx, t);
+    if (S->stage) cudaFreeHost(S->stage);
     cudaSetDevice(prev);
     delete S;
     return RF_OK;
