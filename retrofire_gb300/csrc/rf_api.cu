@@ -116,7 +116,7 @@ struct rf_ctx {
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
-    DevBuf triw, trib, scan64, rowtot, rows, rprims, jstats;
+    DevBuf triw, trib, scan64, rowtot, rows, rprims, live, jstats;
     DevBuf lrec, lmask;  // line pass
     // CUDA graphs of the launch sequence, keyed by frame shape (graph mode).
     bool graphs = false;
@@ -566,6 +566,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->scan64, rfk::scan64_scratch_words((uint32_t)nt) * 8))) return st;
     if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
     if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
+    if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 4))) return st;
     if (!ctx->rows_need_host) {
         CK(cudaMallocHost(&ctx->rows_need_host, sizeof(unsigned long long)));
         CK(cudaEventCreateWithFlags(&ctx->rows_evt, cudaEventDisableTiming));
@@ -643,11 +644,10 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(mark(RF_STAGE_SETUP));
         CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
                              P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
-                             P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), counters + RF_CNT_PRIMS,
-                             P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
+                             P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
                              P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
-                             P<uint32_t>(ctx->mask), kst, counters, ctx->nsm, s));
+                             P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), kst, counters, ctx->nsm, s));
         CK(mark(RF_STAGE_RASTER));
         CK(rfk::launch_raster(TW, kind, fast, jd, nj, dd, P<PrimRec>(ctx->prims),
                               P<RasterPrim>(ctx->rprims), P<uint32_t>(ctx->rows), P<uint32_t>(ctx->tcnt),
@@ -806,7 +806,7 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
-                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->jstats, &ctx->lrec, &ctx->lmask};
+                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->jstats, &ctx->lrec, &ctx->lmask};
     if (ctx->rows_need_host) cudaFreeHost(ctx->rows_need_host);
     if (ctx->rows_evt) cudaEventDestroy(ctx->rows_evt);
     for (DevBuf *b : bufs) cudaFree(b->p);

@@ -496,9 +496,13 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const float4 *__restrict__ cpos, const uint32_t *__restrict__ tcnt,
                         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ tpoly,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
-                        uint32_t *__restrict__ tri_words, StatsDev *__restrict__ stats) {
+                        uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
+                        uint32_t *__restrict__ live, uint32_t *__restrict__ live_n,
+                        StatsDev *__restrict__ stats) {
     // Each thread builds its record in shared memory; the warp then writes
-    // the records out with coalesced 16-byte stores.
+    // the records out with coalesced 16-byte stores.  Only triangles that
+    // pass the face-cull test get a record, and their indices are appended
+    // to the live list the binning pass walks.
     __shared__ __align__(16) PrimRec srec[RF_SETUP_THREADS];
     const uint32_t lane = threadIdx.x & 31, wbase = threadIdx.x & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -525,6 +529,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
         uint32_t words = 0;  // row-record words of this input triangle so far
         for (uint32_t c = 0; c < maxc; ++c) {
             const bool have = c < cnt;
+            bool keep = false;  // passes the face-cull test
             if (have) {
                 const DrawDev &d = draws[di];
                 const JobDev &J = jobs[job];
@@ -562,15 +567,24 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 const bool backface = wz < 0.0f;
                 const bool culled = (J.face_cull == RF_K_CULL_BACK && backface) ||
                                     (J.face_cull == RF_K_CULL_FRONT && !backface);
+                keep = !culled;
+                if (culled && cnt > 1) {
+                    // A piece of a clipped triangle: the rasteriser walks
+                    // every piece of a triangle it meets and skips this one.
+                    RasterPrim *R = rprims + p0 + c;
+                    R->draw = di;
+                    R->flags = 0u;
+                    R->kind = d.shader;
+                }
+                if (!culled) {
                 PrimRec &P = srec[threadIdx.x];
                 P.draw = di;
-                P.live = culled ? 0u : 1u;
+                P.live = 1u;
                 P.tri = gt;
                 P.kind = d.shader;
                 P.rloc = words;
                 P.rwords = 0;
                 P.job = job;
-                if (!culled) {
                 prims_o += 1;
                 // raster.rs:185-224 tri_fill: stable sort by y (total_cmp).
                 SV v0 = sv[0], v1 = sv[1], v2 = sv[2], tmp;
@@ -612,9 +626,16 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 }
             }
             __syncwarp();
-            // Write out the records built in this round, one per pass.
-            uint32_t bal = __ballot_sync(0xFFFFFFFFu, have);
+            uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
             const uint32_t dst = p0 + c;
+            if (bal) {  // append this round's live triangles to the list
+                const uint32_t lead = __ffs(bal) - 1;
+                uint32_t at = 0;
+                if (lane == lead) at = atomicAdd(live_n, (uint32_t)__popc(bal));
+                at = __shfl_sync(0xFFFFFFFFu, at, lead);
+                if (keep) live[at + __popc(bal & ((1u << lane) - 1u))] = dst;
+            }
+            // Write out the records built in this round, one per pass.
             while (bal) {
                 const uint32_t l = __ffs(bal) - 1;
                 bal &= bal - 1;
@@ -689,21 +710,23 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_
 
 __global__ void __launch_bounds__(256, 4)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
-      PrimRec *__restrict__ prims, const uint32_t *__restrict__ nprims_dev, uint32_t tile_w,
+      PrimRec *__restrict__ prims, const uint32_t *__restrict__ live, uint32_t tile_w,
       const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
       unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
       StatsDev *__restrict__ stats, uint32_t *__restrict__ counters) {
     const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t np = *nprims_dev;
+    // Only the triangles that passed the face-cull test (the live list, in
+    // no particular order: every output below depends on the triangle alone).
+    const uint32_t nl = counters[RF_CNT_LIVE];
     // Two record slots per warp of the 256-thread block: the next triangle's
     // record is copied (cp.async) while the current one is walked.
     __shared__ __align__(16) PrimRec srec[8][2];
     __shared__ __align__(16) RasterPrim srp[8];
     __shared__ float stab[8][32][RF_NR + 1];   // scanline values of one band
-    auto fetch = [&](PrimRec *dst, uint32_t p) {
-        if (p < np) {
+    auto fetch = [&](PrimRec *dst, uint32_t p, bool ok) {
+        if (ok) {
             const char *src = reinterpret_cast<const char *>(prims + p);
             for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) {
                 const uint32_t sa = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char *>(dst) + q * 16);
@@ -714,7 +737,11 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
     uint32_t cur = 0;
-    fetch(&srec[wib][0], wid);
+    // Live-list entries: this warp's current and next triangle (the one
+    // after that is loaded one iteration ahead).
+    uint32_t pc = wid < nl ? __ldg(live + wid) : 0u;
+    uint32_t pn = wid + nw < nl ? __ldg(live + wid + nw) : 0u;
+    fetch(&srec[wib][0], pc, wid < nl);
     RasterPrim *R = &srp[wib];
     float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -741,11 +768,15 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
         }
     };
-    for (uint32_t p = wid; p < np; p += nw) {
+    for (uint32_t i = wid; i < nl; i += nw) {
+        const uint32_t pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : 0u;
         __syncwarp();  // the other slot's previous triangle is done
-        fetch(&srec[wib][cur ^ 1u], p + nw);
+        fetch(&srec[wib][cur ^ 1u], pn, i + nw < nl);
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncwarp();
+        const uint32_t p = pc;
+        pc = pn;
+        pn = pnn;
         PrimRec *sP = &srec[wib][cur];
         cur ^= 1u;
         if (lane == 0) {
@@ -996,16 +1027,19 @@ size_t scan64_scratch_words(uint32_t n) {
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, const uint32_t *nprims_dev, uint32_t *tri_words,
+                         PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, StatsDev *stats, uint32_t *counters,
-                         int nsm, cudaStream_t s) {
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, StatsDev *stats,
+                         uint32_t *counters, int nsm, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(counters + RF_CNT_LIVE, 0, 4, s);
+    if (e != cudaSuccess) return e;
     uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
-                                                prims, tri_words, stats);
-    cudaError_t e = cudaGetLastError();
+                                                prims, tri_words, rprims, live,
+                                                counters + RF_CNT_LIVE, stats);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // Row-record offsets of the input triangles (64-bit: the total may not fit 32).
     const uint32_t nb = (nt + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS);
@@ -1014,9 +1048,9 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     k_scan64_add<<<nb, SCAN_THREADS, 0, s>>>(tri_wbase, nt, scan64);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    // one warp per output triangle; the count is only known on the device
+    // one warp per live output triangle; the count is only known on the device
     uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
-    k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, nprims_dev, tile_w, tri_wbase, rows, rows_cap,
+    k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap,
                                   rprims, mask, stats, counters);
     return cudaGetLastError();
 }

@@ -45,6 +45,7 @@
 #define RF_CNT_PRIMS 4    // total output prims (scan total)
 #define RF_CNT_QUEUE 5    // tile queue head
 #define RF_CNT_ROWSOVF 6  // triangles rasterised without row records (buffer full)
+#define RF_CNT_LIVE 7     // output triangles that passed the face-cull test
 #define RF_CNT_N 8
 
 namespace rfk {
@@ -57,19 +58,20 @@ size_t scan_scratch_words(uint32_t n);
 cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch,
                         uint32_t *total, cudaStream_t s);
 // Triangle setup (k_setup), the scan of row-record sizes, then scanline
-// statistics, row records and tile binning (k_bin).  nprims_dev = the
-// device-side total of output triangles; tri_words (nt u32), tri_wbase (nt
+// statistics, row records and tile binning (k_bin).  tri_words (nt u32), tri_wbase (nt
 // u64) and scan64 (scan64_scratch_words(nt) u64) are scratch; rows holds
-// rows_cap words; rows_total receives the words the frame asked for.
+// rows_cap words; rows_total receives the words the frame asked for; live
+// (room for every output triangle) receives the indices of the triangles
+// that pass the face-cull test, counters[RF_CNT_LIVE] their number.
 size_t scan64_scratch_words(uint32_t n);
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, const uint32_t *nprims_dev, uint32_t *tri_words,
+                         PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, StatsDev *stats, uint32_t *counters,
-                         int nsm, cudaStream_t s);
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, StatsDev *stats,
+                         uint32_t *counters, int nsm, cudaStream_t s);
 // kind: the shader kind shared by every draw of the jobs, or RF_K_ANY;
 // fast: every job uses the default context on a target with depth.
 cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,

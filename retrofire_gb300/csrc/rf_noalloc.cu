@@ -59,8 +59,9 @@ constexpr size_t OFF_TRIB = al(OFF_TRIW + (size_t)RF_NOALLOC_MAX_TRIS * 4);
 constexpr size_t OFF_SCAN64 = al(OFF_TRIB + (size_t)RF_NOALLOC_MAX_TRIS * 8);
 constexpr size_t OFF_ROWTOT = al(OFF_SCAN64 + 64 * 8);
 constexpr size_t OFF_RPRIMS = al(OFF_ROWTOT + 8);
-constexpr size_t OFF_ROWS =
+constexpr size_t OFF_LIVE =
     al(OFF_RPRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(RasterPrim));
+constexpr size_t OFF_ROWS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 4);
 // The rest of the area holds row records; triangles whose records do not
 // fit are rasterised from their setup records instead (same results).
 constexpr size_t ROWS_WORDS = (RF_NOALLOC_SCRATCH_BYTES - OFF_ROWS) / 4;
@@ -208,6 +209,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     unsigned long long *scan64 = reinterpret_cast<unsigned long long *>(base + OFF_SCAN64);
     unsigned long long *rowtot = reinterpret_cast<unsigned long long *>(base + OFF_ROWTOT);
     RasterPrim *rprims = reinterpret_cast<RasterPrim *>(base + OFF_RPRIMS);
+    uint32_t *live = reinterpret_cast<uint32_t *>(base + OFF_LIVE);
     uint32_t *rows = reinterpret_cast<uint32_t *>(base + OFF_ROWS);
 
     // ---- zero what the kernels accumulate into, then the pass itself
@@ -226,8 +228,8 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
                                cnt, nsm, s));
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
-                                cnt + RF_CNT_PRIMS, triw, trib, scan64, rowtot, rows, ROWS_WORDS,
-                                rprims, mask, sd, cnt, nsm, s));
+                                triw, trib, scan64, rowtot, rows, ROWS_WORDS, rprims, mask, live,
+                                sd, cnt, nsm, s));
         const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
                           flags->depth_write;
         NA_CK(rfk::launch_raster(TILE_W, shader, fast, jd, 1, dd, prims, rprims, rows, tcnt, toff,
