@@ -674,7 +674,12 @@ namespace {
 // k steps of Iter::next on the first N components, side by side.
 template <int N>
 __device__ __forceinline__ void step_k(float *v, const float *d, uint32_t k) {
-    for (uint32_t i = 0; i < k; ++i) {
+    uint32_t i = 0;
+    for (; i + 4u <= k; i += 4u) {  // four additions per trip, the same sequence
+#pragma unroll
+        for (int c = 0; c < N; ++c) v[c] = fadd(fadd(fadd(fadd(v[c], d[c]), d[c]), d[c]), d[c]);
+    }
+    for (; i < k; ++i) {
 #pragma unroll
         for (int c = 0; c < N; ++c) v[c] = fadd(v[c], d[c]);
     }
@@ -717,6 +722,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t tw_log2 = __ffs(tile_w) - 1;  // tile widths are powers of two
     // Only the triangles that passed the face-cull test (the live list, in
     // no particular order: every output below depends on the triangle alone).
     const uint32_t nl = counters[RF_CNT_LIVE];
@@ -763,7 +769,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, sft));
         }
         if (lo < hi) {
-            const uint32_t t0 = lo / tile_w, t1 = (hi - 1) / tile_w;
+            const uint32_t t0 = lo >> tw_log2, t1 = (hi - 1) >> tw_log2;
             uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
             for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
         }
@@ -857,7 +863,16 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                         const int64_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
                         if (lane < nr) {
                             const uint32_t m = (uint32_t)(ye - ys + 1);
-                            for (uint32_t i = 0; i < m; ++i) {
+                            uint32_t i = 0;
+                            for (; i + 4u <= m; i += 4u) {  // four rows per trip
+                                const float w1 = fadd(wv, wd), w2 = fadd(w1, wd), w3 = fadd(w2, wd);
+                                T[i][lane] = wv;
+                                T[i + 1][lane] = w1;
+                                T[i + 2][lane] = w2;
+                                T[i + 3][lane] = w3;
+                                wv = fadd(w3, wd);
+                            }
+                            for (; i < m; ++i) {
                                 T[i][lane] = wv;
                                 wv = fadd(wv, wd);
                             }
@@ -888,7 +903,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                             // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102),
                             // and the varyings at the span's first tile boundary.
                             const float tshift = fsub(x0r, lx);
-                            const uint32_t kb = w0 ? (o.px0 / tile_w + 1) * tile_w - o.px0 : 0u;
+                            const uint32_t kb = w0 ? tile_w - (o.px0 & (tile_w - 1u)) : 0u;
                             const bool crosses = w0 && o.px0 + kb < o.px1;
                             const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
                             // The components step side by side (independent

@@ -325,8 +325,7 @@ struct PreNC {
 };
 __host__ __device__ constexpr uint32_t row_words(int nc) { return 1u + 2u * (uint32_t)nc; }
 
-// Word indices of RasterPrim fields (the header travels as 24 words, word k
-// in lane k, while it is in flight).
+// Word indices of RasterPrim fields.
 #define RF_RPW_FLAGS 1
 #define RF_RPW_BASE 3
 #define RF_RPW_STRIDE 4
@@ -340,19 +339,15 @@ static_assert(offsetof(RasterPrim, flags) == 4 * RF_RPW_FLAGS && offsetof(Raster
                   offsetof(RasterPrim, c1) == 4 * RF_RPW_C1,
               "RasterPrim word layout");
 
-// Row records of one triangle whose header is spread over the warp (word k
-// of the header in lane k's hw); present = the triangle exists.  Every lane
-// calls this together (the fields are shuffled out of hw).
+// Row records of one triangle whose header H sits in shared memory;
+// present = the triangle exists.  Every lane calls this together.
 template <int KIND>
-__device__ __forceinline__ void stage_rows(const TileCtx &T, uint32_t *slot, bool present, uint32_t hw,
-                                           const uint32_t *__restrict__ rows) {
-    const uint32_t flags = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_FLAGS);
-    const uint32_t rbase = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_BASE);
-    const uint32_t stride = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_STRIDE);  // 1 + 2 NC of its own kind
-    const uint32_t y0 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_Y0);
-    const uint32_t c0 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_C0);
-    const uint32_t y1 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_Y1);
-    const uint32_t c1 = __shfl_sync(0xFFFFFFFFu, hw, RF_RPW_C1);
+__device__ __forceinline__ void stage_rows(const TileCtx &T, uint32_t *slot, bool present,
+                                           const RasterPrim *H, const uint32_t *__restrict__ rows) {
+    const uint32_t flags = H->flags;
+    const uint32_t rbase = H->base;
+    const uint32_t stride = H->stride;  // 1 + 2 NC of its own kind
+    const uint32_t y0 = H->y0, c0 = H->c0, y1 = H->y1, c1 = H->c1;
     uint32_t *dst = slot + T.lane;
     if (!present || !T.row_ok || (flags & (RF_RP_LIVE | RF_RP_ROWS)) != (RF_RP_LIVE | RF_RP_ROWS)) {
         dst[0] = 0u;
@@ -558,15 +553,15 @@ __device__ __forceinline__ void wait_staged_but() {
 
 }  // namespace rfr
 
-// Shared-memory words per warp: colour and depth tiles, three staged
-// triangle headers, the depth-segment minima.
-// Pipeline distances of the rasteriser: a triangle's header is loaded into
-// registers RF_HDR_AHEAD triangles before its turn, its row records are
-// copied into shared memory RF_ROW_AHEAD before (a ring of RF_ROW_SLOTS);
-// the header of the current triangle sits in one shared-memory slot.
+// Shared-memory words per warp: colour and depth tiles, the ring of staged
+// triangle headers, the ring of staged row records, the depth-segment minima.
+// Pipeline distances of the rasteriser: a triangle's header is copied into
+// shared memory RF_HDR_AHEAD triangles before its turn (a ring of
+// RF_HDR_SLOTS), its row records RF_ROW_AHEAD before (a ring of
+// RF_ROW_SLOTS).
 #define RF_HDR_AHEAD 8
 #define RF_ROW_AHEAD 2
-#define RF_HDR_SLOTS 1u
+#define RF_HDR_SLOTS (RF_HDR_AHEAD + 1u)
 #define RF_ROW_SLOTS (RF_ROW_AHEAD + 1u)
 template <int TW, int KIND>
 __host__ __device__ constexpr uint32_t raster_warp_words() {
@@ -668,55 +663,56 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         it.lane = lane;
         it.init();
         // Software pipeline over the tile's triangles t0, t1, ...: iteration
-        // i rasterises t_i while the headers of t_{i+1} .. t_{i+HA} are in
-        // flight or held in registers (hw[k]: word `lane` of t_{i+k}'s
-        // header; ordinary loads, so a register waits only when it is used)
-        // and the row records of t_{i+1} .. t_{i+RA} are in flight as
-        // cp.async groups, one per triangle in order.  Iteration i commits
-        // the group of t_{i+RA}; the rows of t_i are then complete once all
-        // but the newest RA groups are.
+        // i rasterises t_i while the headers of t_{i+1} .. t_{i+HA} and the
+        // row records of t_{i+1} .. t_{i+RA} are in flight (cp.async into
+        // the shared-memory rings).  Iteration i issues the header of
+        // t_{i+HA} and the rows of t_{i+RA} as one commit group G_i, then
+        // waits for all but the newest RA groups: the rows of t_i (G_{i-RA})
+        // and every header up to t_{i+HA-RA} are then complete.  The rows of
+        // t_{i+RA} need its header, from G_{i+RA-HA}, complete by the wait of
+        // iteration i-1 since HA >= 2 RA + 1.
         constexpr uint32_t NONE = 0xFFFFFFFFu;
         constexpr int HA = RF_HDR_AHEAD, RA = RF_ROW_AHEAD;
-        constexpr uint32_t HWN = sizeof(RasterPrim) / 4;
-        static_assert(RA >= 1 && HA >= RA && HWN <= 32, "pipeline shape");
-        const uint32_t *rpw = reinterpret_cast<const uint32_t *>(rprims);
-        auto hload = [&](uint32_t t) -> uint32_t {
-            return t != NONE && lane < HWN ? __ldg(rpw + (size_t)t * HWN + lane) : 0u;
-        };
-        uint32_t q[HA + 1];   // t_i .. t_{i+HA}
-        uint32_t hw[HA + 1];  // their header words
+        constexpr uint32_t HS = RF_HDR_SLOTS;
+        static_assert(RA >= 1 && HA >= 2 * RA + 1 && HS == (uint32_t)HA + 1u, "pipeline shape");
+        uint32_t q[HA + 1];  // t_i .. t_{i+HA}
         q[0] = it.next();
         if (q[0] != NONE) {
             load_tile_and_bounds();
             loaded = true;
 #pragma unroll
             for (int k = 1; k <= HA; ++k) q[k] = q[k - 1] != NONE ? it.next() : NONE;
+            // Headers of t_0 .. t_{HA-1} (t_{HA} comes with G_0), waited
+            // for at once before the first row records are staged.
 #pragma unroll
-            for (int k = 0; k <= HA; ++k) hw[k] = hload(q[k]);
+            for (int k = 0; k < HA; ++k)
+                if (q[k] != NONE) stage_prim(stage + k, rprims + q[k], lane);
+            commit_stage();
+            wait_staged_but<0>();
 #pragma unroll
             for (int k = 0; k < RA; ++k) {
-                stage_rows<KIND>(T, rslots + k * RW, q[k] != NONE, hw[k], rows);
+                stage_rows<KIND>(T, rslots + k * RW, q[k] != NONE, stage + k, rows);
                 commit_stage();
             }
             uint32_t r = 0;  // row slot of t_i (mod RA+1)
+            uint32_t h = 0;  // header slot of t_i (mod HA+1)
             for (;;) {
-                const uint32_t rr = r == 0 ? RF_ROW_SLOTS - 1 : r - 1;  // t_{i+RA}: t_{i-1}'s old slot
-                stage_rows<KIND>(T, rslots + rr * RW, q[RA] != NONE, hw[RA], rows);
+                const uint32_t hn = h == 0 ? HS - 1 : h - 1;                // t_{i+HA}: t_{i-1}'s old slot
+                const uint32_t hr = h + RA >= HS ? h + RA - HS : h + RA;    // t_{i+RA}
+                const uint32_t rr = r == 0 ? RF_ROW_SLOTS - 1 : r - 1;      // t_{i+RA}: t_{i-1}'s old slot
+                if (q[HA] != NONE) stage_prim(stage + hn, rprims + q[HA], lane);
+                stage_rows<KIND>(T, rslots + rr * RW, q[RA] != NONE, stage + hr, rows);
                 commit_stage();
-                if (lane < HWN) reinterpret_cast<uint32_t *>(stage)[lane] = hw[0];
                 wait_staged_but<RA>();
-                raster_prim<KIND, FAST>(T, draws, stage, prims + q[0], rslots + r * RW);
+                raster_prim<KIND, FAST>(T, draws, stage + h, prims + q[0], rslots + r * RW);
                 __syncwarp();
                 if (q[1] == NONE) break;
                 const uint32_t qn = q[HA] != NONE ? it.next() : NONE;
 #pragma unroll
-                for (int k = 0; k < HA; ++k) {
-                    q[k] = q[k + 1];
-                    hw[k] = hw[k + 1];
-                }
+                for (int k = 0; k < HA; ++k) q[k] = q[k + 1];
                 q[HA] = qn;
-                hw[HA] = hload(qn);
                 r = r + 1 == RF_ROW_SLOTS ? 0 : r + 1;
+                h = h + 1 == HS ? 0 : h + 1;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
             __syncwarp();
