@@ -340,6 +340,22 @@ void graphs_drop(rf_ctx *ctx) {
     ctx->gcache.clear();
 }
 
+// Word offsets of every job's tile masks and, after all of them, of the
+// tiles' summary words (one bit per mask word); returns the words in all.
+uint64_t layout_masks(std::vector<JobDev> &hj) {
+    uint64_t w = 0;
+    for (JobDev &J : hj) {
+        J.mask_base = w;
+        w += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
+    }
+    for (JobDev &J : hj) {
+        J.sum_words = (J.mask_words + 31) / 32;
+        J.sum_base = w;
+        w += (uint64_t)J.tiles_x * J.tiles_y * J.sum_words;
+    }
+    return w;
+}
+
 // Validates every draw of every job and fills ctx->hdraws / ctx->hjobs.
 // Nothing is queued on the GPU and no state changes on failure.
 rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<JobHost> &host,
@@ -440,6 +456,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
         h.slot = (int32_t)hj.size();
         hj.push_back(J);
     }
+    layout_masks(hj);
     nv_out = nv;
     nt_out = nt;
     return RF_OK;
@@ -458,6 +475,7 @@ rf_status retile(std::vector<JobDev> &hj, uint32_t TW) {
         mask_words += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
         if (tiles > 0xFFFFFFF0ull) return RF_ERR_BAD_ARG;
     }
+    layout_masks(hj);
     return RF_OK;
 }
 
@@ -545,7 +563,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     ctx->last_tile_w = TW;
     const JobDev &JL = hj.back();
     const uint32_t ntiles = JL.tile_base + JL.tiles_x * JL.tiles_y;
-    const size_t mask_words = JL.mask_base + (size_t)JL.tiles_x * JL.tiles_y * JL.mask_words;
+    const size_t mask_words = JL.sum_base + (size_t)JL.tiles_x * JL.tiles_y * JL.sum_words;  // masks + summaries
     const uint32_t ndraws = (uint32_t)hd.size();
 
     if ((st = ensure(ctx, ctx->draws, hd.size() * sizeof(DrawDev)))) return st;

@@ -52,7 +52,8 @@ struct JobDev {
     uint32_t clear_flags;     // bit0: colour clear pending, bit1: depth clear pending
     uint32_t clear_px;
     float clear_z;
-    uint32_t pad_;
+    uint32_t sum_words;       // summary words per tile: bit b of word s = mask word 32 s + b is nonzero
+    uint64_t sum_base;        // word offset of the job's tile-0 summary (after every job's masks)
     float vp[16];             // Mat4<Ndc, Screen>
 };
 

@@ -771,7 +771,13 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         if (lo < hi) {
             const uint32_t t0 = lo >> tw_log2, t1 = (hi - 1) >> tw_log2;
             uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
-            for (uint32_t t = t0 + lane; t <= t1; t += 32) atomicOr(row + (size_t)t * J.mask_words, bit);
+            // ... and the summary bit of that mask word
+            uint32_t *srow = mask + J.sum_base + (size_t)band * J.tiles_x * J.sum_words + (word >> 5);
+            const uint32_t sbit = 1u << (word & 31u);
+            for (uint32_t t = t0 + lane; t <= t1; t += 32) {
+                atomicOr(row + (size_t)t * J.mask_words, bit);
+                atomicOr(srow + (size_t)t * J.sum_words, sbit);
+            }
         }
     };
     for (uint32_t i = wid; i < nl; i += nw) {

@@ -38,6 +38,7 @@ constexpr uint32_t WARPS = 4;
 constexpr uint32_t MAX_TILES = ((RF_NOALLOC_MAX_W + TILE_W - 1) / TILE_W) *
                                ((RF_NOALLOC_MAX_H + RF_TILE_H - 1) / RF_TILE_H);
 constexpr uint32_t MASK_WORDS = (RF_NOALLOC_MAX_TRIS + 31) / 32;
+constexpr uint32_t SUM_WORDS = (MASK_WORDS + 31) / 32;
 
 // Layout of the scratch area (byte offsets, 256-byte aligned).
 constexpr size_t OFF_DRAW = 0;
@@ -54,7 +55,7 @@ constexpr size_t OFF_POOL = al(OFF_SCAN + 64 * 4);
 constexpr size_t OFF_PRIMS =
     al(OFF_POOL + (size_t)RF_NOALLOC_MAX_TRIS * RF_POLY_STORE * sizeof(PolyVert));
 constexpr size_t OFF_MASK = al(OFF_PRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(PrimRec));
-constexpr size_t OFF_TRIW = al(OFF_MASK + (size_t)MAX_TILES * MASK_WORDS * 4);
+constexpr size_t OFF_TRIW = al(OFF_MASK + (size_t)MAX_TILES * (MASK_WORDS + SUM_WORDS) * 4);
 constexpr size_t OFF_TRIB = al(OFF_TRIW + (size_t)RF_NOALLOC_MAX_TRIS * 4);
 constexpr size_t OFF_SCAN64 = al(OFF_TRIB + (size_t)RF_NOALLOC_MAX_TRIS * 8);
 constexpr size_t OFF_ROWTOT = al(OFF_SCAN64 + 64 * 8);
@@ -179,6 +180,9 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     J.tiles_y = (h + RF_TILE_H - 1) / RF_TILE_H;
     J.ntri = ntri;
     J.mask_words = (ntri + 31) / 32;
+    J.mask_base = 0;
+    J.sum_words = (J.mask_words + 31) / 32;
+    J.sum_base = (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;  // summaries after the masks
     if (clear_rgba) {
         J.clear_flags |= 1u;
         J.clear_px = pack(*clear_rgba, pixfmt);
@@ -222,7 +226,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     } else {
         NA_CK(cudaMemcpyAsync(dd, &d, sizeof d, cudaMemcpyHostToDevice, s));
         NA_CK(cudaMemcpyAsync(jd, &J, sizeof J, cudaMemcpyHostToDevice, s));
-        NA_CK(cudaMemsetAsync(mask, 0, (size_t)ntiles * J.mask_words * 4, s));
+        NA_CK(cudaMemsetAsync(mask, 0, (size_t)ntiles * (J.mask_words + J.sum_words) * 4, s));
         NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, nsm, s));
         NA_CK(rfk::launch_clip(dd, 1, ntri, cpos, coc, tcnt, tpoly, pool, RF_NOALLOC_MAX_TRIS,
                                cnt, nsm, s));

@@ -445,50 +445,88 @@ __device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restric
 
 // Walks a tile's bitmask in submission order: set bits of the mask words
 // (input triangles), each expanded to its clipped output triangles.  The
-// next 32 input triangles are gathered at once, lane k holding the k-th
-// one's output range (toff, tcnt loaded in parallel), so one load latency
-// covers 32 triangles.  Warp-uniform state; every lane calls next() together.
+// tile's summary words (one bit per nonzero mask word) are read 128 at a
+// time; the nonzero mask words they name are then fetched 32 at a time
+// (lane e loads entry e), so an empty stretch of the mask costs nothing.
+// The next 32 input triangles are gathered at once, lane k holding the
+// k-th one's output range (toff, tcnt loaded in parallel), so one load
+// latency covers 32 triangles.  Warp-uniform state; every lane calls
+// next() together.
 struct PrimIter {
-    const uint32_t *tmask;
+    const uint32_t *tmask;  // the tile's mask words
+    const uint32_t *tsum;   // the tile's summary words
     const uint32_t *toff;
     const uint32_t *tcnt;
-    uint32_t nwords, tri_base, lane;
-    // Mask words are read 128 at a time (lane L holds words wb + 32 c + L,
-    // c = 0..3) so one load round covers four ballots.
-    uint32_t wb, w1, w2, w3, word, chunk, bal, src, wv, p, pend;
+    uint32_t nsum, tri_base, lane;
+    // Summary words: lane L holds words sb + 32 c + L, c = 0..3.
+    uint32_t sb, s1, s2, s3, sword, schunk, sbal, ssrc, sv;
+    // Gathered mask words: lane e holds entry e (index widx, value wval).
+    uint32_t widx, wval, wn, wi;
+    uint32_t cur, curw;  // bits left of the current mask word, its index
+    uint32_t p, pend;
     uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
     bool started;
+    // Index of the next nonzero mask word, or false.
+    __device__ __forceinline__ bool next_word(uint32_t &w) {
+        for (;;) {
+            if (sv) {
+                const uint32_t b = __ffs(sv) - 1;
+                sv &= sv - 1;
+                w = (sb + schunk * 32 + ssrc) * 32 + b;
+                return true;
+            }
+            if (sbal) {
+                ssrc = __ffs(sbal) - 1;
+                sbal &= sbal - 1;
+                sv = __shfl_sync(0xFFFFFFFFu, sword, ssrc);
+                continue;
+            }
+            if (started && schunk < 3) {
+                ++schunk;
+                sword = schunk == 1 ? s1 : (schunk == 2 ? s2 : s3);
+                sbal = __ballot_sync(0xFFFFFFFFu, sword != 0u);
+                continue;
+            }
+            if (started) sb += 128;
+            started = true;
+            if (sb >= nsum) return false;
+            const uint32_t i0 = sb + lane;
+            sword = i0 < nsum ? tsum[i0] : 0u;
+            s1 = i0 + 32 < nsum ? tsum[i0 + 32] : 0u;
+            s2 = i0 + 64 < nsum ? tsum[i0 + 64] : 0u;
+            s3 = i0 + 96 < nsum ? tsum[i0 + 96] : 0u;
+            schunk = 0;
+            sbal = __ballot_sync(0xFFFFFFFFu, sword != 0u);
+        }
+    }
+    __device__ __forceinline__ void word_refill() {
+        uint32_t mine = 0, n = 0, w;
+        while (n < 32u && next_word(w)) {
+            if (lane == n) mine = w;
+            ++n;
+        }
+        wn = n;
+        wi = 0;
+        widx = mine;
+        wval = lane < n ? tmask[mine] : 0u;
+    }
     // Next set bit (input triangle, global index) or false.
     __device__ __forceinline__ bool next_bit(uint32_t &gt) {
         for (;;) {
-            if (wv) {
-                const uint32_t b = __ffs(wv) - 1;
-                wv &= wv - 1;
-                gt = tri_base + (wb + chunk * 32 + src) * 32 + b;
+            if (cur) {
+                const uint32_t b = __ffs(cur) - 1;
+                cur &= cur - 1;
+                gt = tri_base + curw * 32 + b;
                 return true;
             }
-            if (bal) {
-                src = __ffs(bal) - 1;
-                bal &= bal - 1;
-                wv = __shfl_sync(0xFFFFFFFFu, word, src);
+            if (wi < wn) {
+                cur = __shfl_sync(0xFFFFFFFFu, wval, wi);
+                curw = __shfl_sync(0xFFFFFFFFu, widx, wi);
+                ++wi;
                 continue;
             }
-            if (started && chunk < 3) {
-                ++chunk;
-                word = chunk == 1 ? w1 : (chunk == 2 ? w2 : w3);
-                bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
-                continue;
-            }
-            if (started) wb += 128;
-            started = true;
-            if (wb >= nwords) return false;
-            const uint32_t i0 = wb + lane;
-            word = i0 < nwords ? tmask[i0] : 0u;
-            w1 = i0 + 32 < nwords ? tmask[i0 + 32] : 0u;
-            w2 = i0 + 64 < nwords ? tmask[i0 + 64] : 0u;
-            w3 = i0 + 96 < nwords ? tmask[i0 + 96] : 0u;
-            chunk = 0;
-            bal = __ballot_sync(0xFFFFFFFFu, word != 0u);
+            word_refill();
+            if (wn == 0) return false;
         }
     }
     __device__ __forceinline__ void refill() {
@@ -505,7 +543,8 @@ struct PrimIter {
         }
     }
     __device__ __forceinline__ void init() {
-        wb = w1 = w2 = w3 = word = chunk = bal = src = wv = p = pend = 0;
+        sb = s1 = s2 = s3 = sword = schunk = sbal = ssrc = sv = 0;
+        widx = wval = wn = wi = cur = curw = p = pend = 0;
         boff = bcnt = bn = bi = 0;
         started = false;
     }
@@ -656,9 +695,10 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         };
         PrimIter it;
         it.tmask = mask + J.mask_base + (size_t)lt * J.mask_words;
+        it.tsum = mask + J.sum_base + (size_t)lt * J.sum_words;
         it.toff = toff;
         it.tcnt = tcnt;
-        it.nwords = J.mask_words;
+        it.nsum = J.sum_words;
         it.tri_base = J.tri_base;
         it.lane = lane;
         it.init();
