@@ -64,6 +64,25 @@ struct Kind {
     static constexpr int NC = KIND == RF_K_FLAT ? 1
                             : KIND == RF_K_TEXTURED ? 3
                             : KIND == RF_K_TEX_GOURAUD ? 6 : 4;
+    static constexpr bool TEXTURED = KIND == RF_K_TEXTURED || KIND == RF_K_TEX_GOURAUD;
+    // The texel a fragment samples (textured kinds; any varyings give an
+    // in-range index), then the colour from it: shade() split in two so
+    // several fragments' texel loads can be in flight together.
+    __device__ static __forceinline__ uint32_t texel(const DrawDev &d, const float *v) {
+        if constexpr (KIND == RF_K_TEXTURED) return sample_tex(d, fdiv(v[1], v[0]), fdiv(v[2], v[0]));
+        else if constexpr (KIND == RF_K_TEX_GOURAUD) return sample_tex(d, fdiv(v[4], v[0]), fdiv(v[5], v[0]));
+        else return 0u;
+    }
+    __device__ static __forceinline__ uint32_t from_texel(uint32_t t, const float *v) {
+        if constexpr (KIND == RF_K_TEX_GOURAUD) {
+            const float tr = fdiv((float)(t & 0xFFu), 256.0f);
+            const float tg = fdiv((float)((t >> 8) & 0xFFu), 256.0f);
+            const float tb = fdiv((float)((t >> 16) & 0xFFu), 256.0f);
+            return to_color4(fmul(tr, v[1]), fmul(tg, v[2]), fmul(tb, v[3]));
+        } else {
+            return t;
+        }
+    }
     __device__ static __forceinline__ uint32_t shade(const DrawDev &d, const float *v) {
         if constexpr (KIND == RF_K_FLAT) {
             return d.flat_rgba;
@@ -131,25 +150,56 @@ __device__ __forceinline__ uint32_t pixels(TileCtx &T, const DrawDev &d, float *
                 v2[c] = fadd(v1[c], dv[c]);
                 v3[c] = fadd(v2[c], dv[c]);
             }
-            if (c0 < v[0]) {  // ctx.rs:86-89 with Some(Less)
-                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
-                T.sdep[idx] = v[0];
-                ++nout;
-            }
-            if (c1 < v1[0]) {
-                T.scol[idx + RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
-                T.sdep[idx + RF_TILE_H] = v1[0];
-                ++nout;
-            }
-            if (c2 < v2[0]) {
-                T.scol[idx + 2 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v2), T.fmt);
-                T.sdep[idx + 2 * RF_TILE_H] = v2[0];
-                ++nout;
-            }
-            if (c3 < v3[0]) {
-                T.scol[idx + 3 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v3), T.fmt);
-                T.sdep[idx + 3 * RF_TILE_H] = v3[0];
-                ++nout;
+            // ctx.rs:86-89 with Some(Less)
+            const bool p0 = c0 < v[0], p1 = c1 < v1[0], p2 = c2 < v2[0], p3 = c3 < v3[0];
+            if constexpr (Kind<KIND>::TEXTURED) {
+                // The passing fragments' texels are loaded together, then used.
+                uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+                if (p0) t0 = Kind<KIND>::texel(d, v);
+                if (p1) t1 = Kind<KIND>::texel(d, v1);
+                if (p2) t2 = Kind<KIND>::texel(d, v2);
+                if (p3) t3 = Kind<KIND>::texel(d, v3);
+                if (p0) {
+                    T.scol[idx] = pack_px(Kind<KIND>::from_texel(t0, v), T.fmt);
+                    T.sdep[idx] = v[0];
+                    ++nout;
+                }
+                if (p1) {
+                    T.scol[idx + RF_TILE_H] = pack_px(Kind<KIND>::from_texel(t1, v1), T.fmt);
+                    T.sdep[idx + RF_TILE_H] = v1[0];
+                    ++nout;
+                }
+                if (p2) {
+                    T.scol[idx + 2 * RF_TILE_H] = pack_px(Kind<KIND>::from_texel(t2, v2), T.fmt);
+                    T.sdep[idx + 2 * RF_TILE_H] = v2[0];
+                    ++nout;
+                }
+                if (p3) {
+                    T.scol[idx + 3 * RF_TILE_H] = pack_px(Kind<KIND>::from_texel(t3, v3), T.fmt);
+                    T.sdep[idx + 3 * RF_TILE_H] = v3[0];
+                    ++nout;
+                }
+            } else {
+                if (p0) {
+                    T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                    T.sdep[idx] = v[0];
+                    ++nout;
+                }
+                if (p1) {
+                    T.scol[idx + RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
+                    T.sdep[idx + RF_TILE_H] = v1[0];
+                    ++nout;
+                }
+                if (p2) {
+                    T.scol[idx + 2 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v2), T.fmt);
+                    T.sdep[idx + 2 * RF_TILE_H] = v2[0];
+                    ++nout;
+                }
+                if (p3) {
+                    T.scol[idx + 3 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v3), T.fmt);
+                    T.sdep[idx + 3 * RF_TILE_H] = v3[0];
+                    ++nout;
+                }
             }
 #pragma unroll
             for (int c = 0; c < NC; ++c) v[c] = fadd(v3[c], dv[c]);
