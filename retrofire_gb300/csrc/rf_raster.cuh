@@ -645,17 +645,23 @@ __device__ __forceinline__ void wait_staged_but() {
 // Shared-memory words per warp: colour and depth tiles, the ring of staged
 // triangle headers, the ring of staged row records, the depth-segment minima.
 // Pipeline distances of the rasteriser: a triangle's header is copied into
-// shared memory RF_HDR_AHEAD triangles before its turn (a ring of
-// RF_HDR_SLOTS), its row records RF_ROW_AHEAD before (a ring of
-// RF_ROW_SLOTS).
-#define RF_HDR_AHEAD 8
-#define RF_ROW_AHEAD 2
-#define RF_HDR_SLOTS (RF_HDR_AHEAD + 1u)
-#define RF_ROW_SLOTS (RF_ROW_AHEAD + 1u)
+// shared memory HA triangles before its turn (a ring of HA + 1 slots), its
+// row records RA before (a ring of RA + 1).
+// Narrow tiles hold fewer pixels per triangle, so their iterations are
+// shorter and the row records are copied further ahead.
+#define RF_ROW_AHEAD_NARROW 2  // tile widths 8 and 16
+#define RF_ROW_AHEAD_WIDE 2    // tile widths 32 and 64
+template <int TW>
+struct Pipe {
+    static constexpr int RA = TW <= 16 ? RF_ROW_AHEAD_NARROW : RF_ROW_AHEAD_WIDE;
+    static constexpr int HA = 2 * RA + 1 > 8 ? 2 * RA + 1 : 8;
+    static constexpr uint32_t HS = (uint32_t)HA + 1u;  // header slots
+    static constexpr uint32_t RS = (uint32_t)RA + 1u;  // row-record slots
+};
 template <int TW, int KIND>
 __host__ __device__ constexpr uint32_t raster_warp_words() {
-    return 2u * TW * RF_TILE_H + RF_HDR_SLOTS * (uint32_t)(sizeof(RasterPrim) / 4) +
-           RF_ROW_SLOTS * rfr::row_words(rfr::PreNC<KIND>::NC) * RF_TILE_H + ((uint32_t)TW / RF_SEG) * RF_TILE_H;
+    return 2u * TW * RF_TILE_H + Pipe<TW>::HS * (uint32_t)(sizeof(RasterPrim) / 4) +
+           Pipe<TW>::RS * rfr::row_words(rfr::PreNC<KIND>::NC) * RF_TILE_H + ((uint32_t)TW / RF_SEG) * RF_TILE_H;
 }
 
 // KIND: shader kind of every draw of the job (or RF_K_ANY); FAST: the
@@ -676,8 +682,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
     uint32_t *scol = smem + warp * WARP_WORDS;
     float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
     RasterPrim *stage = reinterpret_cast<RasterPrim *>(scol + 2 * TW * RF_TILE_H);
-    uint32_t *rslots = scol + 2 * TW * RF_TILE_H + RF_HDR_SLOTS * (sizeof(RasterPrim) / 4);
-    float *smin = reinterpret_cast<float *>(rslots + RF_ROW_SLOTS * RW);
+    uint32_t *rslots = scol + 2 * TW * RF_TILE_H + Pipe<TW>::HS * (sizeof(RasterPrim) / 4);
+    float *smin = reinterpret_cast<float *>(rslots + Pipe<TW>::RS * RW);
     for (;;) {
         uint32_t tile = 0;
         if (lane == 0) tile = atomicAdd(tile_queue, 1u);
@@ -762,8 +768,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         // t_{i+RA} need its header, from G_{i+RA-HA}, complete by the wait of
         // iteration i-1 since HA >= 2 RA + 1.
         constexpr uint32_t NONE = 0xFFFFFFFFu;
-        constexpr int HA = RF_HDR_AHEAD, RA = RF_ROW_AHEAD;
-        constexpr uint32_t HS = RF_HDR_SLOTS;
+        constexpr int HA = Pipe<TW>::HA, RA = Pipe<TW>::RA;
+        constexpr uint32_t HS = Pipe<TW>::HS, RS = Pipe<TW>::RS;
         static_assert(RA >= 1 && HA >= 2 * RA + 1 && HS == (uint32_t)HA + 1u, "pipeline shape");
         uint32_t q[HA + 1];  // t_i .. t_{i+HA}
         q[0] = it.next();
@@ -789,7 +795,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
             for (;;) {
                 const uint32_t hn = h == 0 ? HS - 1 : h - 1;                // t_{i+HA}: t_{i-1}'s old slot
                 const uint32_t hr = h + RA >= HS ? h + RA - HS : h + RA;    // t_{i+RA}
-                const uint32_t rr = r == 0 ? RF_ROW_SLOTS - 1 : r - 1;      // t_{i+RA}: t_{i-1}'s old slot
+                const uint32_t rr = r == 0 ? RS - 1 : r - 1;                // t_{i+RA}: t_{i-1}'s old slot
                 if (q[HA] != NONE) stage_prim(stage + hn, rprims + q[HA], lane);
                 stage_rows<KIND>(T, rslots + rr * RW, q[RA] != NONE, stage + hr, rows);
                 commit_stage();
@@ -801,7 +807,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
 #pragma unroll
                 for (int k = 0; k < HA; ++k) q[k] = q[k + 1];
                 q[HA] = qn;
-                r = r + 1 == RF_ROW_SLOTS ? 0 : r + 1;
+                r = r + 1 == RS ? 0 : r + 1;
                 h = h + 1 == HS ? 0 : h + 1;
             }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
