@@ -116,7 +116,7 @@ struct rf_ctx {
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
-    DevBuf triw, trib, scan64, rowtot, rows, rprims, live, jstats;
+    DevBuf triw, trib, scan64, rowtot, rows, rprims, live, marks, items, jstats;
     DevBuf lrec, lmask;  // line pass
     // CUDA graphs of the launch sequence, keyed by frame shape (graph mode).
     bool graphs = false;
@@ -452,7 +452,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
         memcpy(J.vp, ji.vp, sizeof J.vp);
         tiles += (uint64_t)J.tiles_x * J.tiles_y;
         mask_words += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
-        if (tiles > 0xFFFFFFF0ull) return RF_ERR_BAD_ARG;
+        if (tiles > RF_MAX_TILES) return RF_ERR_BAD_ARG;
         h.slot = (int32_t)hj.size();
         hj.push_back(J);
     }
@@ -473,7 +473,7 @@ rf_status retile(std::vector<JobDev> &hj, uint32_t TW) {
         J.mask_base = mask_words;
         tiles += (uint64_t)J.tiles_x * J.tiles_y;
         mask_words += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
-        if (tiles > 0xFFFFFFF0ull) return RF_ERR_BAD_ARG;
+        if (tiles > RF_MAX_TILES) return RF_ERR_BAD_ARG;
     }
     layout_masks(hj);
     return RF_OK;
@@ -585,6 +585,8 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
     if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
     if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 4))) return st;
+    if ((st = ensure(ctx, ctx->marks, ((size_t)nj + 1) * 8))) return st;
+    if ((st = ensure(ctx, ctx->items, (size_t)ntiles * (RF_SPLIT_K + 1) * 4))) return st;
     if (!ctx->rows_need_host) {
         CK(cudaMallocHost(&ctx->rows_need_host, sizeof(unsigned long long)));
         CK(cudaEventCreateWithFlags(&ctx->rows_evt, cudaEventDisableTiming));
@@ -665,12 +667,15 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                              P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
                              P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
-                             P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), kst, counters, ctx->nsm, s));
+                             P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
+                             nj, kst, counters, ctx->nsm, s));
+        CK(rfk::launch_items(jd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
+                             (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));
         CK(mark(RF_STAGE_RASTER));
         CK(rfk::launch_raster(TW, kind, fast, jd, nj, dd, P<PrimRec>(ctx->prims),
                               P<RasterPrim>(ctx->rprims), P<uint32_t>(ctx->rows), P<uint32_t>(ctx->tcnt),
-                              P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles,
-                              counters + RF_CNT_QUEUE, kst, ctx->warps, ctx->nsm, s));
+                              P<uint32_t>(ctx->toff), P<uint32_t>(ctx->mask), ntiles, P<uint32_t>(ctx->items),
+                              counters + RF_CNT_ITEMS, counters + RF_CNT_QUEUE, kst, ctx->warps, ctx->nsm, s));
         CK(mark(RF_STAGE_N));
         if (per_job) CK(rfk::launch_stats_fold(kst, nj, P<StatsDev>(ctx->stats), s));
         return RF_OK;
@@ -721,8 +726,8 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(cudaEventRecord(tuned->e1, s));
         tuned->pending = true;
     }
-    // vertex, clip, 3 scan, setup, 3 scan64, bin, raster (+ the stats fold)
-    ctx->kernels += 11 + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
+    // vertex, clip, 3 scan, setup, 3 scan64, bin, work list, raster (+ the stats fold)
+    ctx->kernels += 12 + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -824,7 +829,7 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
-                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->jstats, &ctx->lrec, &ctx->lmask};
+                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->marks, &ctx->items, &ctx->jstats, &ctx->lrec, &ctx->lmask};
     if (ctx->rows_need_host) cudaFreeHost(ctx->rows_need_host);
     if (ctx->rows_evt) cudaEventDestroy(ctx->rows_evt);
     for (DevBuf *b : bufs) cudaFree(b->p);

@@ -498,7 +498,8 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
                         uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
                         uint32_t *__restrict__ live, uint32_t *__restrict__ live_n,
-                        StatsDev *__restrict__ stats) {
+                        uint32_t *__restrict__ extra, StatsDev *__restrict__ stats) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *extra = 0;  // the work list's counter
     // Each thread builds its record in shared memory; the warp then writes
     // the records out with coalesced 16-byte stores.  Only triangles that
     // pass the face-cull test get a record, and their indices are appended
@@ -718,7 +719,8 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
       PrimRec *__restrict__ prims, const uint32_t *__restrict__ live, uint32_t tile_w,
       const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
       unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
-      StatsDev *__restrict__ stats, uint32_t *__restrict__ counters) {
+      StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
+      unsigned long long *__restrict__ jmarks, uint32_t nj) {
     const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -752,12 +754,17 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
     unsigned long long acc_fi = 0, acc_oob = 0;  // per-lane, for cur_job
+    uint32_t acc_marks = 0;                        // (triangle, tile) bits set by this lane
+    unsigned long long all_marks = 0;  // every job's, for the frame total
     auto flush = [&]() {
         if (cur_job != 0xFFFFFFFFu) {
             warp_add_u64(&stats[cur_job].frags_i, acc_fi, true);
             warp_add_u64(&stats[cur_job].oob, acc_oob, true);
+            warp_add_u64(&jmarks[cur_job], acc_marks, true);
         }
+        all_marks += acc_marks;
         acc_fi = acc_oob = 0;
+        acc_marks = 0;
     };
     // One band of the target: reduce the lanes' covered columns and mark the
     // band's tiles with this triangle's bit.
@@ -777,6 +784,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             for (uint32_t t = t0 + lane; t <= t1; t += 32) {
                 atomicOr(row + (size_t)t * J.mask_words, bit);
                 atomicOr(srow + (size_t)t * J.sum_words, sbit);
+                ++acc_marks;
             }
         }
     };
@@ -993,6 +1001,58 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         }
     }
     flush();
+    warp_add_u64(&jmarks[nj], all_marks, true);
+}
+
+// The rasteriser's work list.  A tile walks its triangles serially, so the
+// tiles that take longest should start first, and a tile far more crowded
+// than the rest (the horizon of a scene of many small objects) would close
+// the pass alone: such a tile is split into RF_SPLIT_K items, one per slice
+// of RF_TILE_H / RF_SPLIT_K rows, walked by different warps (each pixel
+// still sees its triangles in order: a row belongs to one slice).  The list
+// is items[ntiles ..) -- the heavy tiles and the slices of the crowded ones,
+// in no particular order -- then items[0 .. ntiles) -- every tile in index
+// order, RF_ITEM_SKIP where the tile went to the first part.
+//
+// k_tile_items: one warp per tile.  Its nonzero mask words (the set bits
+// of its summary words) stand for its triangle count: at most the count,
+// about it where the tile's triangles are scattered through the submission
+// order.  A crowded tile is one whose nonzero words alone exceed four times
+// its scene's mean (marks / tiles: an outlier of its own scene) and the
+// frame's marks per resident warp (its walk alone outlasts a warp's fair
+// share of the pass, so splitting it shortens the pass).
+#define RF_SPLIT_MIN 64u  // a tile with fewer binned triangles is never split
+#define RF_HEAVY_MIN 16u  // ... nor taken early
+__global__ void __launch_bounds__(256)
+k_tile_items(const JobDev *__restrict__ jobs, uint32_t nj, const uint32_t *__restrict__ mask,
+             uint32_t ntiles, const unsigned long long *__restrict__ jmarks, uint32_t slots,
+             uint32_t *__restrict__ items, uint32_t *__restrict__ extra) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (tile >= ntiles) return;
+    const uint32_t ji = upper_index(nj, tile, [&](uint32_t i) { return jobs[i].tile_base; });
+    const JobDev &J = jobs[ji];
+    const uint32_t lt = tile - J.tile_base;
+    const uint32_t *sw = mask + J.sum_base + (size_t)lt * J.sum_words;
+    uint32_t c = 0;
+    for (uint32_t i = lane; i < J.sum_words; i += 32) c += __popc(sw[i]);
+    c = __reduce_add_sync(0xFFFFFFFFu, c);
+    if (lane == 0) {
+        const unsigned long long mean4 = 4ull * jmarks[ji] / ((unsigned long long)J.tiles_x * J.tiles_y);
+        const unsigned long long share = jmarks[nj] / slots;
+        const uint32_t thr =
+            (uint32_t)min(max(max((unsigned long long)RF_SPLIT_MIN, mean4), share), 0xFFFFFFFFull);
+        const bool crowded = c > thr;
+        // Heavy: more than twice the frame's mean; taken before the rest.
+        const bool heavy = crowded || (c > RF_HEAVY_MIN && c > 2ull * jmarks[nj] / ntiles);
+        items[tile] = heavy ? RF_ITEM_SKIP : tile * 8u;
+        if (crowded) {
+            const uint32_t at = ntiles + atomicAdd(extra, RF_SPLIT_K);
+            for (uint32_t k = 1; k <= RF_SPLIT_K; ++k) items[at + k - 1] = tile * 8u + k;
+        } else if (heavy) {
+            items[ntiles + atomicAdd(extra, 1u)] = tile * 8u;
+        }
+    }
 }
 
 // Frame::clear applied directly (when no render follows before a read).
@@ -1051,15 +1111,18 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, StatsDev *stats,
-                         uint32_t *counters, int nsm, cudaStream_t s) {
-    if (nt == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(counters + RF_CNT_LIVE, 0, 4, s);
-    if (e != cudaSuccess) return e;
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *jmarks,
+                         uint32_t nj, StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(jmarks, 0, ((size_t)nj + 1) * 8, s)) != cudaSuccess) return e;
+    if (nt == 0)  // no setup pass to zero the work-list counter
+        return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
+    if ((e = cudaMemsetAsync(counters + RF_CNT_LIVE, 0, 4, s)) != cudaSuccess) return e;
     uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
                                                 prims, tri_words, rprims, live,
-                                                counters + RF_CNT_LIVE, stats);
+                                                counters + RF_CNT_LIVE, counters + RF_CNT_ITEMS,
+                                                stats);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // Row-record offsets of the input triangles (64-bit: the total may not fit 32).
@@ -1072,21 +1135,31 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     // one warp per live output triangle; the count is only known on the device
     uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
     k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap,
-                                  rprims, mask, stats, counters);
+                                  rprims, mask, stats, counters, jmarks, nj);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_items(const JobDev *jobs, uint32_t nj, const uint32_t *mask, uint32_t ntiles,
+                         const unsigned long long *jmarks, uint32_t slots, uint32_t *items,
+                         uint32_t *counters, cudaStream_t s) {
+    if (ntiles == 0) return cudaSuccess;
+    k_tile_items<<<(uint32_t)(((uint64_t)ntiles * 32 + 255) / 256), 256, 0, s>>>(
+        jobs, nj, mask, ntiles, jmarks, slots ? slots : 1u, items, counters + RF_CNT_ITEMS);
     return cudaGetLastError();
 }
 
 cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,
                           const DrawDev *draws, const PrimRec *prims, const RasterPrim *rprims,
                           const uint32_t *rows, const uint32_t *tcnt, const uint32_t *toff,
-                          const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
+                          const uint32_t *mask, uint32_t ntiles, const uint32_t *items, const uint32_t *nitems,
+                          uint32_t *queue,
                           StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     switch (tile_w) {
-        case 8: return launch_raster_tw8(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        case 16: return launch_raster_tw16(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        case 64: return launch_raster_tw64(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
-        default: return launch_raster_tw32(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        case 8: return launch_raster_tw8(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
+        case 16: return launch_raster_tw16(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
+        case 64: return launch_raster_tw64(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
+        default: return launch_raster_tw32(kind, fast, jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
     }
 }
 

@@ -46,7 +46,8 @@
 #define RF_CNT_QUEUE 5    // tile queue head
 #define RF_CNT_ROWSOVF 6  // triangles rasterised without row records (buffer full)
 #define RF_CNT_LIVE 7     // output triangles that passed the face-cull test
-#define RF_CNT_N 8
+#define RF_CNT_ITEMS 8    // rasteriser work items after the first ntiles (slices of crowded tiles)
+#define RF_CNT_N 16
 
 namespace rfk {
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
@@ -62,7 +63,8 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 // u64) and scan64 (scan64_scratch_words(nt) u64) are scratch; rows holds
 // rows_cap words; rows_total receives the words the frame asked for; live
 // (room for every output triangle) receives the indices of the triangles
-// that pass the face-cull test, counters[RF_CNT_LIVE] their number.
+// that pass the face-cull test, counters[RF_CNT_LIVE] their number; jmarks
+// (nj + 1) receives each scene's (triangle, tile) bits, then their sum.
 size_t scan64_scratch_words(uint32_t n);
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
@@ -70,22 +72,35 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, StatsDev *stats,
-                         uint32_t *counters, int nsm, cudaStream_t s);
-// kind: the shader kind shared by every draw of the jobs, or RF_K_ANY;
-// fast: every job uses the default context on a target with depth.
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *jmarks,
+                         uint32_t nj, StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s);
+// The rasteriser's work list from the tile masks and the scenes' marks
+// (slots: the warps the rasteriser keeps resident, about).  items (room
+// for (RF_SPLIT_K + 1) * ntiles): items[ntiles .. ntiles + extra) first --
+// heavy tiles (tile * 8) and the row slices of crowded tiles (tile * 8 + k,
+// k = 1 .. RF_SPLIT_K) -- then items[0 .. ntiles): tile t * 8 in index
+// order, RF_ITEM_SKIP for the tiles already listed; extra is
+// counters[RF_CNT_ITEMS] (zeroed by launch_setup).
+cudaError_t launch_items(const JobDev *jobs, uint32_t nj, const uint32_t *mask, uint32_t ntiles,
+                         const unsigned long long *jmarks, uint32_t slots, uint32_t *items,
+                         uint32_t *counters, cudaStream_t s);
+#define RF_SPLIT_K 4  // row slices of a crowded tile (RF_TILE_H / RF_SPLIT_K rows each)
+#define RF_ITEM_SKIP 0xFFFFFFFEu  // a work-list entry taken elsewhere in the list
+#define RF_MAX_TILES (1u << 28)  // tiles of one frame or batch (work items hold tile * 8 + k)
 cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,
                           const DrawDev *draws, const PrimRec *prims, const RasterPrim *rprims,
                           const uint32_t *rows, const uint32_t *tcnt, const uint32_t *toff,
-                          const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
+                          const uint32_t *mask, uint32_t ntiles, const uint32_t *items, const uint32_t *nitems,
+                          uint32_t *queue,
                           StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s);
 #define RF_DECL_RASTER_TW(TW)                                                                  \
     cudaError_t launch_raster_tw##TW(int kind, bool fast, const JobDev *jobs, uint32_t nj,      \
                                      const DrawDev *draws, const PrimRec *prims,                \
                                      const RasterPrim *rprims, const uint32_t *rows,            \
                                      const uint32_t *tcnt, const uint32_t *toff,                \
-                                     const uint32_t *mask, uint32_t ntiles, uint32_t *queue,    \
-                                     StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s);
+                                     const uint32_t *mask, uint32_t ntiles, const uint32_t *items, \
+                                     const uint32_t *nitems, uint32_t *queue, StatsDev *stats,    \
+                                     uint32_t warps, int nsm, cudaStream_t s);
 RF_DECL_RASTER_TW(8)
 RF_DECL_RASTER_TW(16)
 RF_DECL_RASTER_TW(32)

@@ -62,7 +62,9 @@ constexpr size_t OFF_ROWTOT = al(OFF_SCAN64 + 64 * 8);
 constexpr size_t OFF_RPRIMS = al(OFF_ROWTOT + 8);
 constexpr size_t OFF_LIVE =
     al(OFF_RPRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(RasterPrim));
-constexpr size_t OFF_ROWS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 4);
+constexpr size_t OFF_MARKS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 4);
+constexpr size_t OFF_ITEMS = al(OFF_MARKS + 16);
+constexpr size_t OFF_ROWS = al(OFF_ITEMS + (size_t)MAX_TILES * (RF_SPLIT_K + 1) * 4);
 // The rest of the area holds row records; triangles whose records do not
 // fit are rasterised from their setup records instead (same results).
 constexpr size_t ROWS_WORDS = (RF_NOALLOC_SCRATCH_BYTES - OFF_ROWS) / 4;
@@ -214,6 +216,8 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     unsigned long long *rowtot = reinterpret_cast<unsigned long long *>(base + OFF_ROWTOT);
     RasterPrim *rprims = reinterpret_cast<RasterPrim *>(base + OFF_RPRIMS);
     uint32_t *live = reinterpret_cast<uint32_t *>(base + OFF_LIVE);
+    unsigned long long *marks = reinterpret_cast<unsigned long long *>(base + OFF_MARKS);
+    uint32_t *items = reinterpret_cast<uint32_t *>(base + OFF_ITEMS);
     uint32_t *rows = reinterpret_cast<uint32_t *>(base + OFF_ROWS);
 
     // ---- zero what the kernels accumulate into, then the pass itself
@@ -233,11 +237,12 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
                                 triw, trib, scan64, rowtot, rows, ROWS_WORDS, rprims, mask, live,
-                                sd, cnt, nsm, s));
+                                marks, 1, sd, cnt, nsm, s));
+        NA_CK(rfk::launch_items(jd, 1, mask, ntiles, marks, (uint32_t)nsm * 16u, items, cnt, s));
         const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
                           flags->depth_write;
         NA_CK(rfk::launch_raster(TILE_W, shader, fast, jd, 1, dd, prims, rprims, rows, tcnt, toff,
-                                 mask, ntiles,
+                                 mask, ntiles, items, cnt + RF_CNT_ITEMS,
                                  cnt + RF_CNT_QUEUE, sd, WARPS, nsm, s));
     }
     if (stats) {

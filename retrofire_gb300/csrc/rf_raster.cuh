@@ -515,6 +515,9 @@ struct PrimIter {
     uint32_t cur, curw;  // bits left of the current mask word, its index
     uint32_t p, pend;
     uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
+    uint32_t keep;                // entries of the batch to walk
+    const RasterPrim *rprims;
+    uint32_t slo, shi;            // rows of a row-slice item (slo >= shi: the whole tile)
     bool started;
     // Index of the next nonzero mask word, or false.
     __device__ __forceinline__ bool next_word(uint32_t &w) {
@@ -587,15 +590,27 @@ struct PrimIter {
         }
         bn = n;
         bi = 0;
+        bool take = lane < n;
         if (lane < n) {
             boff = __ldg(toff + mine);
             bcnt = __ldg(tcnt + mine);
+            if (slo < shi && bcnt == 1u) {
+                // A row slice of a crowded tile: an unclipped triangle whose
+                // rows miss the slice is passed over here.
+                const uint32_t *h = reinterpret_cast<const uint32_t *>(rprims + boff);
+                const uint32_t fl = __ldg(h + RF_RPW_FLAGS);
+                const uint32_t y0 = __ldg(h + RF_RPW_Y0), c0 = __ldg(h + RF_RPW_C0);
+                const uint32_t y1 = __ldg(h + RF_RPW_Y1), c1 = __ldg(h + RF_RPW_C1);
+                if (fl & RF_RP_ROWS)
+                    take = (c0 && y0 < shi && y0 + c0 > slo) || (c1 && y1 < shi && y1 + c1 > slo);
+            }
         }
+        keep = __ballot_sync(0xFFFFFFFFu, take);
     }
     __device__ __forceinline__ void init() {
         sb = s1 = s2 = s3 = sword = schunk = sbal = ssrc = sv = 0;
         widx = wval = wn = wi = cur = curw = p = pend = 0;
-        boff = bcnt = bn = bi = 0;
+        boff = bcnt = bn = bi = keep = 0;
         started = false;
     }
     __device__ __forceinline__ uint32_t next() {
@@ -603,6 +618,10 @@ struct PrimIter {
             if (bi >= bn) {
                 refill();
                 if (bn == 0) return 0xFFFFFFFFu;
+            }
+            if (!((keep >> bi) & 1u)) {
+                ++bi;
+                continue;
             }
             p = __shfl_sync(0xFFFFFFFFu, boff, bi);
             pend = p + __shfl_sync(0xFFFFFFFFu, bcnt, bi);
@@ -673,7 +692,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
          const PrimRec *__restrict__ prims, const RasterPrim *__restrict__ rprims,
          const uint32_t *__restrict__ rows, const uint32_t *__restrict__ tcnt,
          const uint32_t *__restrict__ toff, const uint32_t *__restrict__ mask,
-         uint32_t ntiles_total, uint32_t *__restrict__ tile_queue, StatsDev *__restrict__ stats) {
+         uint32_t ntiles_total, const uint32_t *__restrict__ items, const uint32_t *__restrict__ nitems_dev,
+         uint32_t *__restrict__ tile_queue, StatsDev *__restrict__ stats) {
     using namespace rfr;
     extern __shared__ __align__(16) uint32_t smem[];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -684,10 +704,22 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
     RasterPrim *stage = reinterpret_cast<RasterPrim *>(scol + 2 * TW * RF_TILE_H);
     uint32_t *rslots = scol + 2 * TW * RF_TILE_H + Pipe<TW>::HS * (sizeof(RasterPrim) / 4);
     float *smin = reinterpret_cast<float *>(rslots + Pipe<TW>::RS * RW);
+    // Queue position q: the heavy tiles and crowded-tile slices first
+    // (items[ntiles + q]), then every other tile in index order.
+    const uint32_t nfirst = *nitems_dev;
+    const uint32_t nitems = ntiles_total + nfirst;
     for (;;) {
-        uint32_t tile = 0;
-        if (lane == 0) tile = atomicAdd(tile_queue, 1u);
-        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
+        uint32_t item = 0;
+        if (lane == 0) {
+            do {
+                const uint32_t pos = atomicAdd(tile_queue, 1u);
+                item = pos >= nitems ? 0xFFFFFFFFu
+                                     : items[pos < nfirst ? ntiles_total + pos : pos - nfirst];
+            } while (item == RF_ITEM_SKIP);
+        }
+        item = __shfl_sync(0xFFFFFFFFu, item, 0);
+        if (item == 0xFFFFFFFFu) break;
+        const uint32_t tile = item >> 3, slice = item & 7u;  // slice 0: the whole tile
         if (tile >= ntiles_total) break;
         const uint32_t ji = upper_index(nj, tile, [&](uint32_t i) { return jobs[i].tile_base; });
         const JobDev &J = jobs[ji];
@@ -702,7 +734,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         T.tx1 = min(T.tx0 + (uint32_t)TW, J.w);
         T.tw = TW;
         T.y = tyi * RF_TILE_H + lane;
-        T.row_ok = T.y < J.h;
+        constexpr uint32_t SLICE_H = RF_TILE_H / RF_SPLIT_K;
+        T.row_ok = T.y < J.h && (slice == 0 || lane / SLICE_H == slice - 1u);
         T.has_depth = J.depth != nullptr;
         T.depth_test = J.depth_test;
         T.color_write = J.color_write != 0;
@@ -755,6 +788,9 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         it.toff = toff;
         it.tcnt = tcnt;
         it.nsum = J.sum_words;
+        it.rprims = rprims;
+        it.slo = slice ? tyi * RF_TILE_H + (slice - 1u) * SLICE_H : 0u;
+        it.shi = slice ? it.slo + SLICE_H : 0u;
         it.tri_base = J.tri_base;
         it.lane = lane;
         it.init();
@@ -849,8 +885,8 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
                                    const PrimRec *prims, const RasterPrim *rprims,
                                    const uint32_t *rows, const uint32_t *tcnt,
                                    const uint32_t *toff, const uint32_t *mask, uint32_t ntiles,
-                                   uint32_t *queue, StatsDev *stats, uint32_t warps, int nsm,
-                                   cudaStream_t s) {
+                                   const uint32_t *items, const uint32_t *nitems, uint32_t *queue,
+                                   StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
     // Shared memory per block: at most the 227 KB opt-in limit, so the
     // block takes as many warps as fit (wide tiles of the generic kind).
     constexpr size_t SMEM_MAX = 227 * 1024;
@@ -866,11 +902,11 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster<TW, KIND, FAST>, warps * 32, smem);
     if (per_sm < 1) per_sm = 1;
     uint32_t blocks = (uint32_t)per_sm * (uint32_t)nsm;
-    const uint32_t need = (ntiles + warps - 1) / warps;
+    const uint32_t need = (ntiles + warps - 1) / warps;  // (a few crowded-tile slices more are shared out)
     if (blocks > need) blocks = need;
     if (blocks == 0) blocks = 1;
     k_raster<TW, KIND, FAST><<<blocks, warps * 32, smem, s>>>(jobs, nj, draws, prims, rprims, rows,
-                                                             tcnt, toff, mask, ntiles, queue, stats);
+                                                             tcnt, toff, mask, ntiles, items, nitems, queue, stats);
     return cudaGetLastError();
 }
 
@@ -882,23 +918,24 @@ static cudaError_t launch_raster_for_width(int kind, bool fast, const JobDev *jo
                                            const DrawDev *draws, const PrimRec *prims,
                                            const RasterPrim *rprims, const uint32_t *rows,
                                            const uint32_t *tcnt, const uint32_t *toff,
-                                           const uint32_t *mask, uint32_t ntiles, uint32_t *queue,
+                                           const uint32_t *mask, uint32_t ntiles, const uint32_t *items, const uint32_t *nitems,
+                          uint32_t *queue,
                                            StatsDev *stats, uint32_t warps, int nsm, cudaStream_t s) {
     if (!fast)
-        return launch_raster_k<TW, RF_K_ANY, false>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+        return launch_raster_k<TW, RF_K_ANY, false>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
     switch (kind) {
         case RF_K_FLAT:
-            return launch_raster_k<TW, RF_K_FLAT, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_FLAT, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
         case RF_K_GOURAUD:
-            return launch_raster_k<TW, RF_K_GOURAUD, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_GOURAUD, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
         case RF_K_TEXTURED:
-            return launch_raster_k<TW, RF_K_TEXTURED, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_TEXTURED, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
         case RF_K_TEX_GOURAUD:
-            return launch_raster_k<TW, RF_K_TEX_GOURAUD, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_TEX_GOURAUD, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
         case RF_K_GOURAUD_SRGB:
-            return launch_raster_k<TW, RF_K_GOURAUD_SRGB, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_GOURAUD_SRGB, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
         default:
-            return launch_raster_k<TW, RF_K_ANY, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, queue, stats, warps, nsm, s);
+            return launch_raster_k<TW, RF_K_ANY, true>(jobs, nj, draws, prims, rprims, rows, tcnt, toff, mask, ntiles, items, nitems, queue, stats, warps, nsm, s);
     }
 }
 
