@@ -646,13 +646,12 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     const JobDev *jd = P<JobDev>(ctx->jobs);
     auto enqueue = [&](bool marks) -> rf_status {
         auto mark = [&](int i) -> cudaError_t { return marks ? cudaEventRecord(ev[i], s) : cudaSuccess; };
-        CK(cudaMemsetAsync(counters + RF_CNT_POOL, 0, 4, s));
-        CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
         CK(cudaMemsetAsync(ctx->mask.p, 0, mask_words * 4, s));
         if (per_job) CK(cudaMemsetAsync(kst, 0, nj * sizeof(StatsDev), s));
         CK(mark(RF_STAGE_VERTEX));
         if (any_cull) CK(rfk::launch_cull(P<DrawDev>(ctx->draws), ndraws, kst, ctx->nsm, s));
         CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                              counters, P<unsigned long long>(ctx->marks), nj + 1,
                               ctx->nsm, s));
         CK(mark(RF_STAGE_CLIP));
         CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
@@ -726,8 +725,9 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(cudaEventRecord(tuned->e1, s));
         tuned->pending = true;
     }
-    // vertex, clip, 3 scan, setup, 3 scan64, bin, work list, raster (+ the stats fold)
-    ctx->kernels += 12 + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
+    // vertex, clip, scan (3, or 1 for one block), setup, scan64 (the same), bin,
+    // work list, raster (+ the stats fold)
+    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 8 : 12) + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -1038,7 +1038,7 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
         CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
         CK(cudaMemsetAsync(ctx->lmask.p, 0, mwords * 4, s));
         CK(rfk::launch_vertex(P<DrawDev>(ctx->draws), 1, m.nverts, P<float4>(ctx->cpos),
-                              P<uint8_t>(ctx->coc), ctx->nsm, s));
+                              P<uint8_t>(ctx->coc), nullptr, nullptr, 0, ctx->nsm, s));
         CK(rfk::launch_lines(P<DrawDev>(ctx->draws), P<JobDev>(ctx->jobs), m.ntri, P<float4>(ctx->cpos),
                              P<uint8_t>(ctx->coc), P<LineRec>(ctx->lrec), P<uint32_t>(ctx->lmask), ntiles,
                              counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->nsm, s));

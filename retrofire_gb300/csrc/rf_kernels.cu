@@ -60,7 +60,17 @@ __device__ __forceinline__ uint32_t zdiv_mask_of(int32_t shader) {
 // and outcode (clip.rs:240-242, 303-309).
 // ---------------------------------------------------------------------------
 __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t nv_total,
-                         float4 *__restrict__ cpos, uint8_t *__restrict__ coc) {
+                         float4 *__restrict__ cpos, uint8_t *__restrict__ coc,
+                         uint32_t *__restrict__ counters, unsigned long long *__restrict__ jmarks,
+                         uint32_t njm) {
+    if (blockIdx.x == 0) {  // the frame's counters, for the kernels after this one
+        if (counters && threadIdx.x == 0) {
+            counters[RF_CNT_POOL] = 0;
+            counters[RF_CNT_QUEUE] = 0;
+            counters[RF_CNT_LIVE] = 0;
+        }
+        for (uint32_t j = threadIdx.x; j < njm; j += blockDim.x) jmarks[j] = 0;
+    }
     // Warp-uniform loop (the draw lookup is shared by the warp's lanes).
     for (uint32_t wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wbase < nv_total;
          wbase += gridDim.x * blockDim.x) {
@@ -254,8 +264,12 @@ __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t 
 // ---------------------------------------------------------------------------
 #define SCAN_THREADS 1024
 #define SCAN_ITEMS 4
+static_assert(SCAN_THREADS * SCAN_ITEMS == RF_SCAN_BLOCK_ITEMS, "scan block size");
+// Exclusive scan of each block's SCAN_THREADS * SCAN_ITEMS values; the block
+// totals go to block_sums, and with a single block the total to *total.
 __global__ void k_scan_blocks(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
-                              uint32_t n, uint32_t *__restrict__ block_sums) {
+                              uint32_t n, uint32_t *__restrict__ block_sums,
+                              uint32_t *__restrict__ total) {
     __shared__ uint32_t warp_sums[32];
     const uint32_t base = blockIdx.x * (SCAN_THREADS * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
     uint32_t v[SCAN_ITEMS], s = 0;
@@ -281,7 +295,10 @@ __global__ void k_scan_blocks(const uint32_t *__restrict__ in, uint32_t *__restr
             if (lane >= (uint32_t)o) wi += y;
         }
         warp_sums[lane] = wi - ws;
-        if (lane == 31) block_sums[blockIdx.x] = wi;
+        if (lane == 31) {
+            block_sums[blockIdx.x] = wi;
+            if (gridDim.x == 1) *total = wi;
+        }
     }
     __syncthreads();
     uint32_t run = warp_sums[wid] + incl - s;
@@ -339,7 +356,8 @@ __global__ void k_scan_add(uint32_t *__restrict__ out, uint32_t n, const uint32_
 
 // Exclusive scan of u32 values into u64 (row-record offsets).
 __global__ void k_scan64_blocks(const uint32_t *__restrict__ in, unsigned long long *__restrict__ out,
-                                uint32_t n, unsigned long long *__restrict__ block_sums) {
+                                uint32_t n, unsigned long long *__restrict__ block_sums,
+                                unsigned long long *__restrict__ total) {
     __shared__ unsigned long long warp_sums[32];
     const uint32_t base = blockIdx.x * (SCAN_THREADS * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
     unsigned long long v[SCAN_ITEMS], s = 0;
@@ -365,7 +383,10 @@ __global__ void k_scan64_blocks(const uint32_t *__restrict__ in, unsigned long l
             if (lane >= (uint32_t)o) wi += y;
         }
         warp_sums[lane] = wi - ws;
-        if (lane == 31) block_sums[blockIdx.x] = wi;
+        if (lane == 31) {
+            block_sums[blockIdx.x] = wi;
+            if (gridDim.x == 1) *total = wi;
+        }
     }
     __syncthreads();
     unsigned long long run = warp_sums[wid] + incl - s;
@@ -1071,10 +1092,11 @@ __global__ void k_fill(uint32_t *__restrict__ color, float *__restrict__ depth, 
 namespace rfk {
 
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
-                          uint8_t *coc, int nsm, cudaStream_t s) {
+                          uint8_t *coc, uint32_t *counters, unsigned long long *jmarks, uint32_t njm,
+                          int nsm, cudaStream_t s) {
     if (nv == 0) return cudaSuccess;
     uint32_t blocks = min((nv + 255) / 256, (uint32_t)nsm * 16);
-    k_vertex<<<blocks, 256, 0, s>>>(draws, nd, nv, cpos, coc);
+    k_vertex<<<blocks, 256, 0, s>>>(draws, nd, nv, cpos, coc, counters, jmarks, njm);
     return cudaGetLastError();
 }
 
@@ -1095,9 +1117,11 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
                         uint32_t *total, cudaStream_t s) {
     if (n == 0) return cudaMemsetAsync(total, 0, 4, s);
     const uint32_t nb = (n + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS);
-    k_scan_blocks<<<nb, SCAN_THREADS, 0, s>>>(in, out, n, scratch);
-    k_scan_sums<<<1, 1024, 0, s>>>(scratch, nb, total);
-    k_scan_add<<<nb, SCAN_THREADS, 0, s>>>(out, n, scratch);
+    k_scan_blocks<<<nb, SCAN_THREADS, 0, s>>>(in, out, n, scratch, total);
+    if (nb > 1) {  // one block: its scan is the whole scan
+        k_scan_sums<<<1, 1024, 0, s>>>(scratch, nb, total);
+        k_scan_add<<<nb, SCAN_THREADS, 0, s>>>(out, n, scratch);
+    }
     return cudaGetLastError();
 }
 
@@ -1114,10 +1138,8 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *jmarks,
                          uint32_t nj, StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s) {
     cudaError_t e;
-    if ((e = cudaMemsetAsync(jmarks, 0, ((size_t)nj + 1) * 8, s)) != cudaSuccess) return e;
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
-    if ((e = cudaMemsetAsync(counters + RF_CNT_LIVE, 0, 4, s)) != cudaSuccess) return e;
     uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
                                                 prims, tri_words, rprims, live,
@@ -1127,9 +1149,11 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     if (e != cudaSuccess) return e;
     // Row-record offsets of the input triangles (64-bit: the total may not fit 32).
     const uint32_t nb = (nt + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS);
-    k_scan64_blocks<<<nb, SCAN_THREADS, 0, s>>>(tri_words, tri_wbase, nt, scan64);
-    k_scan64_sums<<<1, 1024, 0, s>>>(scan64, nb, rows_total);
-    k_scan64_add<<<nb, SCAN_THREADS, 0, s>>>(tri_wbase, nt, scan64);
+    k_scan64_blocks<<<nb, SCAN_THREADS, 0, s>>>(tri_words, tri_wbase, nt, scan64, rows_total);
+    if (nb > 1) {
+        k_scan64_sums<<<1, 1024, 0, s>>>(scan64, nb, rows_total);
+        k_scan64_add<<<nb, SCAN_THREADS, 0, s>>>(tri_wbase, nt, scan64);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // one warp per live output triangle; the count is only known on the device

@@ -48,10 +48,14 @@
 #define RF_CNT_LIVE 7     // output triangles that passed the face-cull test
 #define RF_CNT_ITEMS 8    // rasteriser work items after the first ntiles (slices of crowded tiles)
 #define RF_CNT_N 16
+#define RF_SCAN_BLOCK_ITEMS 4096u  // values one scan block takes (one launch instead of three)
 
 namespace rfk {
+// counters (optional): POOL, QUEUE and LIVE zeroed for the kernels after
+// it, and jmarks[0 .. njm) (the binning pass's per-scene marks).
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
-                          uint8_t *coc, int nsm, cudaStream_t s);
+                          uint8_t *coc, uint32_t *counters, unsigned long long *jmarks, uint32_t njm,
+                          int nsm, cudaStream_t s);
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
                         const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, PolyVert *pool,
                         uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s);

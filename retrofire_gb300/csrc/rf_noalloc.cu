@@ -231,7 +231,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
         NA_CK(cudaMemcpyAsync(dd, &d, sizeof d, cudaMemcpyHostToDevice, s));
         NA_CK(cudaMemcpyAsync(jd, &J, sizeof J, cudaMemcpyHostToDevice, s));
         NA_CK(cudaMemsetAsync(mask, 0, (size_t)ntiles * (J.mask_words + J.sum_words) * 4, s));
-        NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, nsm, s));
+        NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, cnt, marks, 2, nsm, s));
         NA_CK(rfk::launch_clip(dd, 1, ntri, cpos, coc, tcnt, tpoly, pool, RF_NOALLOC_MAX_TRIS,
                                cnt, nsm, s));
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
