@@ -48,14 +48,15 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
     }
 }
 
-// Row quantity r of half H after j scanlines (see HalfRec): one of the two
-// precomputed single-binade runs, else the general loop from the second.
-__device__ __forceinline__ float row_value(const HalfRec *__restrict__ H, int r, uint32_t j) {
-    const uint32_t e0 = H->e0[r];
-    if (j <= e0) return u2f(H->b0[r] + j * (uint32_t)H->i0[r]);
+// Row quantity r of half H after j scanlines (see HalfRuns): one of the two
+// precomputed single-binade runs U, else the general loop from the second.
+__device__ __forceinline__ float row_value(const HalfRec *__restrict__ H, const HalfRuns *__restrict__ U,
+                                           int r, uint32_t j) {
+    const uint32_t e0 = U->e0[r];
+    if (j <= e0) return u2f(H->b0[r] + j * (uint32_t)U->i0[r]);
     const uint32_t j1 = j - e0 - 1u;
-    if (j <= H->e1[r]) return u2f(H->b1[r] + j1 * (uint32_t)H->i1[r]);
-    return seq_add_n(u2f(H->b1[r]), H->d[r], j1);
+    if (j <= U->e1[r]) return u2f(U->b1[r] + j1 * (uint32_t)U->i1[r]);
+    return seq_add_n(u2f(U->b1[r]), H->d[r], j1);
 }
 
 }  // namespace rfd

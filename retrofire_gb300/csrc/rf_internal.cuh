@@ -14,6 +14,7 @@
 #ifndef RF_INTERNAL_CUH
 #define RF_INTERNAL_CUH
 
+#include <stddef.h>
 #include <stdint.h>
 
 #define RF_MAX_ATTR 5        // (Color3f, TexCoord) is the widest varying
@@ -72,11 +73,8 @@ struct PolyVert {
 // One ScanlineIter after scan() (raster.rs:45-51, 248-302): rows y0r,
 // y0r+1, ... (n of them).  Row quantity r (RF_R_LX left edge x, RF_R_RX right
 // edge x, RF_R_C + c interpolated component c: c = 0 screen z, c >= 1 the
-// attributes) is the running sum start + j * d over rows.  Its exact value
-// is kept as two single-binade runs (rfx::fast_params): rows 0..e0[r] have
-// bits b0[r] + j * i0[r]; one explicit addition later, rows e0[r]+1..e1[r]
-// have bits b1[r] + (j - e0[r] - 1) * i1[r]; rows past e1[r] continue from
-// the second run with the general loop.  dvdx = per-pixel step.
+// attributes) is the running sum b0[r] + d[r] + ... over rows; dvdx = the
+// per-pixel step.
 #define RF_R_LX 0
 #define RF_R_RX 1
 #define RF_R_C 2
@@ -85,26 +83,39 @@ struct HalfRec {
     float y0r;
     uint32_t n;
     uint32_t b0[RF_NR];
+    float d[RF_NR];
+    float dvdx[RF_NC];
+};
+
+// The exact value of every row of a half as two single-binade runs
+// (rfx::fast_params): rows 0..e0[r] have bits b0[r] + j * i0[r]; one explicit
+// addition later, rows e0[r]+1..e1[r] have bits b1[r] + (j - e0[r] - 1) *
+// i1[r]; rows past e1[r] continue from the second run with the general loop.
+// Only triangles rasterised without row records need them.
+struct HalfRuns {
     int32_t i0[RF_NR];
     uint32_t e0[RF_NR];
     uint32_t b1[RF_NR];
     int32_t i1[RF_NR];
     uint32_t e1[RF_NR];
-    float d[RF_NR];
-    float dvdx[RF_NC];
 };
 
 struct PrimRec {
     uint32_t draw;
-    uint32_t live;    // 0: culled by the face-cull test
+    uint32_t live;    // 1: passed the face-cull test (only those get a record)
     uint32_t tri;     // global input triangle it was clipped from
     int32_t kind;     // shader kind of its draw
     uint32_t rloc;    // word offset of its row records inside its input triangle's block
     uint32_t rwords;  // words of row records; 0 = rasterised from this record instead
     uint32_t job;     // scene (job) of its draw
     uint32_t pad_;
-    HalfRec half[2];
+    HalfRec half[2];  // what the binning pass reads (RF_PRIM_CORE_BYTES)
+    HalfRuns runs[2]; // written only for a triangle without row records
 };
+#define RF_PRIM_CORE_BYTES 224u
+static_assert(offsetof(PrimRec, runs) == RF_PRIM_CORE_BYTES && RF_PRIM_CORE_BYTES % 16 == 0 &&
+                  sizeof(PrimRec) % 16 == 0,
+              "PrimRec layout");
 
 // Row records: for every scanline of a triangle that lands on a row of the
 // target, word 0 = first pixel | (one past the last pixel) << 16 (the span

@@ -491,21 +491,24 @@ __device__ void scan_setup(float y0, float y1, const SV &l0, const SV &l1, const
 // step (d) are set: run 0 from the first row, run 1 after one explicit
 // addition (rfd::row_value reads them).  Needed only by triangles
 // rasterised without row records.
-__device__ void half_runs(HalfRec &h, uint32_t r) {
+__device__ void half_runs(const HalfRec &h, HalfRuns &u, uint32_t r) {
     uint32_t k0, k1;
-    fast_params(u2f(h.b0[r]), h.d[r], h.i0[r], k0);
-    h.e0[r] = k0;
+    int32_t i0, i1;
+    fast_params(u2f(h.b0[r]), h.d[r], i0, k0);
+    u.i0[r] = i0;
+    u.e0[r] = k0;
     if (k0 == 0xFFFFFFFFu) {  // fixed point: run 0 covers every row
-        h.b1[r] = h.b0[r];
-        h.i1[r] = 0;
-        h.e1[r] = k0;
+        u.b1[r] = h.b0[r];
+        u.i1[r] = 0;
+        u.e1[r] = k0;
         return;
     }
-    const float v1 = fadd(u2f(h.b0[r] + k0 * (uint32_t)h.i0[r]), h.d[r]);
-    fast_params(v1, h.d[r], h.i1[r], k1);
-    h.b1[r] = f2u(v1);
+    const float v1 = fadd(u2f(h.b0[r] + k0 * (uint32_t)i0), h.d[r]);
+    fast_params(v1, h.d[r], i1, k1);
+    u.i1[r] = i1;
+    u.b1[r] = f2u(v1);
     const uint64_t e1 = (uint64_t)k0 + 1u + k1;
-    h.e1[r] = e1 > 0xFFFFFFFEull ? 0xFFFFFFFEu : (uint32_t)e1;
+    u.e1[r] = e1 > 0xFFFFFFFEull ? 0xFFFFFFFEu : (uint32_t)e1;
 }
 
 }  // namespace
@@ -525,7 +528,9 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
     // the records out with coalesced 16-byte stores.  Only triangles that
     // pass the face-cull test get a record, and their indices are appended
     // to the live list the binning pass walks.
-    __shared__ __align__(16) PrimRec srec[RF_SETUP_THREADS];
+    // (the record's first RF_PRIM_CORE_BYTES only: the binade runs, needed
+    // by few triangles, go straight to global memory)
+    __shared__ __align__(16) uint4 sbuf[RF_SETUP_THREADS][RF_PRIM_CORE_BYTES / 16];
     const uint32_t lane = threadIdx.x & 31, wbase = threadIdx.x & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < nt_total; base += stride) {
@@ -599,7 +604,8 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     R->kind = d.shader;
                 }
                 if (!culled) {
-                PrimRec &P = srec[threadIdx.x];
+                // This thread's slot: the fields before `runs` only.
+                PrimRec &P = *reinterpret_cast<PrimRec *>(sbuf[threadIdx.x]);
                 P.draw = di;
                 P.live = 1u;
                 P.tri = gt;
@@ -642,8 +648,9 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     words += (uint32_t)w;
                 }
                 if (P.rwords == 0u) {  // rasterised from this record: it needs the runs
+                    PrimRec *G = prims + p0 + c;
                     for (int hh = 0; hh < 2; ++hh)
-                        for (uint32_t r = 0; r < RF_NR; ++r) half_runs(P.half[hh], r);
+                        for (uint32_t r = 0; r < RF_NR; ++r) half_runs(P.half[hh], G->runs[hh], r);
                 }
                 }
             }
@@ -662,9 +669,9 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 const uint32_t l = __ffs(bal) - 1;
                 bal &= bal - 1;
                 const uint32_t dl = __shfl_sync(0xFFFFFFFFu, dst, l);
-                const uint4 *src = reinterpret_cast<const uint4 *>(&srec[wbase + l]);
+                const uint4 *src = sbuf[wbase + l];
                 uint4 *out = reinterpret_cast<uint4 *>(prims + dl);
-                for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) out[q] = src[q];
+                if (lane < RF_PRIM_CORE_BYTES / 16) out[lane] = src[lane];
             }
             __syncwarp();
         }
@@ -714,10 +721,10 @@ struct RowOut {
 };
 
 // Scanline j of half H landing on row y (< h).
-__device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, uint32_t j, uint32_t w,
-                                          RowOut &o) {
-    const float lx = row_value(H, RF_R_LX, j);
-    const float rx = row_value(H, RF_R_RX, j);
+__device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, const HalfRuns *__restrict__ U,
+                                          uint32_t j, uint32_t w, RowOut &o) {
+    const float lx = row_value(H, U, RF_R_LX, j);
+    const float rx = row_value(H, U, RF_R_RX, j);
     const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
     const uint64_t xs = as_usize_fast(x0r);
     uint64_t xe = as_usize_fast(x1r);
@@ -751,13 +758,13 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     const uint32_t nl = counters[RF_CNT_LIVE];
     // Two record slots per warp of the 256-thread block: the next triangle's
     // record is copied (cp.async) while the current one is walked.
-    __shared__ __align__(16) PrimRec srec[8][2];
+    __shared__ __align__(16) uint4 sbuf[8][2][RF_PRIM_CORE_BYTES / 16];  // records' first parts
     __shared__ __align__(16) RasterPrim srp[8];
     __shared__ float stab[8][32][RF_NR + 1];   // scanline values of one band
-    auto fetch = [&](PrimRec *dst, uint32_t p, bool ok) {
+    auto fetch = [&](uint4 *dst, uint32_t p, bool ok) {
         if (ok) {
             const char *src = reinterpret_cast<const char *>(prims + p);
-            for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) {
+            for (uint32_t q = lane; q < RF_PRIM_CORE_BYTES / 16; q += 32) {
                 const uint32_t sa = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char *>(dst) + q * 16);
                 asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + q * 16)
                              : "memory");
@@ -770,7 +777,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     // after that is loaded one iteration ahead).
     uint32_t pc = wid < nl ? __ldg(live + wid) : 0u;
     uint32_t pn = wid + nw < nl ? __ldg(live + wid + nw) : 0u;
-    fetch(&srec[wib][0], pc, wid < nl);
+    fetch(sbuf[wib][0], pc, wid < nl);
     RasterPrim *R = &srp[wib];
     float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -812,13 +819,13 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     for (uint32_t i = wid; i < nl; i += nw) {
         const uint32_t pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : 0u;
         __syncwarp();  // the other slot's previous triangle is done
-        fetch(&srec[wib][cur ^ 1u], pn, i + nw < nl);
+        fetch(sbuf[wib][cur ^ 1u], pn, i + nw < nl);
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncwarp();
         const uint32_t p = pc;
         pc = pn;
         pn = pnn;
-        PrimRec *sP = &srec[wib][cur];
+        PrimRec *sP = reinterpret_cast<PrimRec *>(sbuf[wib][cur]);  // fields before `runs` only
         cur ^= 1u;
         if (lane == 0) {
             R->draw = sP->draw;
@@ -851,13 +858,9 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                     if (lane == 0) atomicAdd(&counters[RF_CNT_ROWSOVF], 1u);
                     // ... which then needs its binade runs (lane r: quantity r).
                     if (lane < RF_NR) {
-                        half_runs(sP->half[0], lane);
-                        half_runs(sP->half[1], lane);
+                        half_runs(sP->half[0], prims[p].runs[0], lane);
+                        half_runs(sP->half[1], prims[p].runs[1], lane);
                     }
-                    __syncwarp();
-                    const uint4 *src = reinterpret_cast<const uint4 *>(sP);
-                    uint4 *dst = reinterpret_cast<uint4 *>(prims + p);
-                    for (uint32_t q = lane; q < sizeof(PrimRec) / 16; q += 32) dst[q] = src[q];
                     __syncwarp();
                 }
             }
@@ -982,14 +985,15 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                 if (Y < 0) {
                     jfirst = min(in_rows, (int64_t)1 - Y);
                     if (lane == 0)
-                        for (int64_t j = 0; j < jfirst; ++j) row_stats(H, (uint32_t)j, J.w, o0);
+                        for (int64_t j = 0; j < jfirst; ++j)
+                            row_stats(H, &prims[p].runs[hh], (uint32_t)j, J.w, o0);
                 }
                 // Remaining rows y = Y + j > 0 (or all rows when Y >= 0), by band.
                 const int64_t ylo = Y + jfirst, yhi = Y + in_rows - 1;
                 for (int64_t band = (ylo > 0 ? ylo : 0) / RF_TILE_H; band * RF_TILE_H <= yhi; ++band) {
                     const int64_t y = band * RF_TILE_H + lane;
                     RowOut o{0, 0, 0xFFFFFFFFu, 0};
-                    if (y >= ylo && y <= yhi) row_stats(H, (uint32_t)(y - Y), J.w, o);
+                    if (y >= ylo && y <= yhi) row_stats(H, &prims[p].runs[hh], (uint32_t)(y - Y), J.w, o);
                     if (band == 0) {  // fold the rows above the buffer into band 0
                         o.frags_i += o0.frags_i;
                         o.oob += o0.oob;

@@ -281,10 +281,10 @@ __device__ __forceinline__ bool span_hidden(const TileCtx &T, float za, float dz
 // FAST: the default context (depth test Less, colour and depth writes on).
 template <int KIND, bool FAST>
 __device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec *__restrict__ H,
-                                     uint32_t j) {
+                                     const HalfRuns *__restrict__ U, uint32_t j) {
     constexpr int NC = Kind<KIND>::NC;
-    const float lx = row_value(H, RF_R_LX, j);
-    const float rx = row_value(H, RF_R_RX, j);
+    const float lx = row_value(H, U, RF_R_LX, j);
+    const float rx = row_value(H, U, RF_R_RX, j);
     const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
     // xs..xe as `as usize` (target.rs:259-262), zip-truncated to the
     // fragment count, clipped to the tile.  32-bit saturating casts give the
@@ -308,7 +308,7 @@ __device__ __forceinline__ void span(TileCtx &T, const DrawDev &d, const HalfRec
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         dv[c] = H->dvdx[c];
-        const float c0 = row_value(H, RF_R_C + c, j);
+        const float c0 = row_value(H, U, RF_R_C + c, j);
         const float adj = fadd(c0, fmul(fsub(fadd(c0, dv[c]), c0), tshift));
         v[c] = jump(adj, dv[c], k0);
     }
@@ -348,18 +348,20 @@ __device__ __forceinline__ void raster_prim_k(TileCtx &T, const DrawDev &d, cons
     rows_for(&P->half[1], T.y, b0, b1);
     const bool start1 = a1 == a0;
     const HalfRec *H = start1 ? &P->half[1] : &P->half[0];
+    const HalfRuns *U = start1 ? &P->runs[1] : &P->runs[0];
     uint32_t j = start1 ? b0 : a0, jend = start1 ? b1 : a1;
     bool more = !start1 && b1 > b0;
     for (;;) {
         if (j >= jend) {
             if (!more) break;
             H = &P->half[1];
+            U = &P->runs[1];
             j = b0;
             jend = b1;
             more = false;
             continue;
         }
-        span<KIND, FAST>(T, d, H, j);
+        span<KIND, FAST>(T, d, H, U, j);
         ++j;
     }
 }
