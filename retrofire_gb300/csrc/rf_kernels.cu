@@ -869,7 +869,10 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                 R->base = (uint32_t)base;
                 R->stride = stride;
             }
-            uint32_t rec_off = 0;
+            // Both halves' rows, records and dv/dx; a regular triangle's
+            // rows are all on the buffer (row >= 0).
+            int64_t Yh[2] = {0, 0};
+            uint32_t inh[2] = {0u, 0u};
             for (int hh = 0; hh < 2; ++hh) {
                 const HalfRec *H = &P->half[hh];
                 const uint32_t n = H->n;
@@ -885,100 +888,126 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                 const int64_t in_rows = min((int64_t)n, max((int64_t)0, (int64_t)J.h - Y));
                 if (lane == 0) acc_oob += (unsigned long long)((int64_t)n - in_rows);
                 if (in_rows <= 0) continue;
-                if (regular) {
-                    // Scanlines y = Y + j: walked sequentially, one lane per
-                    // row quantity (ScanlineIter::next's running sums), then
-                    // one lane per row for the span, stats and row record.
-                    if (lane == 0) {
-                        if (hh == 0) { R->y0 = (uint32_t)Y; R->c0 = (uint32_t)in_rows; }
-                        else { R->y1 = (uint32_t)Y; R->c1 = (uint32_t)in_rows; }
-                    }
-                    float wv = lane < nr ? u2f(H->b0[lane]) : 0.0f;
-                    const float wd = lane < nr ? H->d[lane] : 0.0f;
-                    const int64_t ylo = Y, yhi = Y + in_rows - 1;
-                    for (int64_t band = ylo / RF_TILE_H; band * RF_TILE_H <= yhi; ++band) {
-                        const int64_t ys = max(ylo, band * RF_TILE_H);
-                        const int64_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
-                        if (lane < nr) {
-                            const uint32_t m = (uint32_t)(ye - ys + 1);
-                            uint32_t i = 0;
-                            for (; i + 4u <= m; i += 4u) {  // four rows per trip
-                                const float w1 = fadd(wv, wd), w2 = fadd(w1, wd), w3 = fadd(w2, wd);
-                                T[i][lane] = wv;
-                                T[i + 1][lane] = w1;
-                                T[i + 2][lane] = w2;
-                                T[i + 3][lane] = w3;
-                                wv = fadd(w3, wd);
-                            }
-                            for (; i < m; ++i) {
-                                T[i][lane] = wv;
-                                wv = fadd(wv, wd);
-                            }
-                        }
-                        __syncwarp();
-                        const int64_t y = band * RF_TILE_H + lane;
-                        RowOut o{0, 0, 0xFFFFFFFFu, 0};
-                        if (y >= ys && y <= ye) {
-                            const uint32_t i = (uint32_t)(y - ys);
-                            const float lx = T[i][RF_R_LX], rx = T[i][RF_R_RX];
-                            const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-                            const uint64_t xs = as_usize_fast(x0r);
-                            uint64_t xe = as_usize_fast(x1r);
-                            if (xe < xs) xe = xs;
-                            o.frags_i = xe - xs;
-                            if (xe > J.w) o.oob = 1;
-                            uint64_t nfr = xe - xs;
-                            const uint32_t cnt = as_u32(fsub(x1r, x0r));
-                            if (cnt < nfr) nfr = cnt;
-                            uint32_t w0 = 0;
-                            if (nfr && xs < J.w) {
-                                o.px0 = (uint32_t)xs;
-                                o.px1 = (uint32_t)(xs + nfr < J.w ? xs + nfr : J.w);
-                                w0 = o.px0 | (o.px1 << 16);
-                            }
-                            uint32_t *rec = rows + base + (size_t)(rec_off + (uint32_t)(y - Y)) * stride;
-                            rec[0] = w0;
-                            // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102),
-                            // and the varyings at the span's first tile boundary.
-                            const float tshift = fsub(x0r, lx);
-                            const uint32_t kb = w0 ? tile_w - (o.px0 & (tile_w - 1u)) : 0u;
-                            const bool crosses = w0 && o.px0 + kb < o.px1;
-                            const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
-                            // The components step side by side (independent
-                            // chains), each exactly like Iter::next.
-                            float vb[RF_NC], dvc[RF_NC];
-#pragma unroll
-                            for (uint32_t c = 0; c < RF_NC; ++c) {
-                                if (c < nc) {
-                                    const float cv = T[i][RF_R_C + c];
-                                    dvc[c] = H->dvdx[c];
-                                    vb[c] = fadd(cv, fmul(fsub(fadd(cv, dvc[c]), cv), tshift));
-                                    rec[1 + c] = f2u(vb[c]);
-                                } else {
-                                    dvc[c] = 0.0f;
-                                    vb[c] = 0.0f;
-                                }
-                            }
-                            switch (nc) {  // only the kind's components step
-                                case 1: step_k<1>(vb, dvc, ksteps); break;
-                                case 2: step_k<2>(vb, dvc, ksteps); break;
-                                case 3: step_k<3>(vb, dvc, ksteps); break;
-                                case 4: step_k<4>(vb, dvc, ksteps); break;
-                                case 5: step_k<5>(vb, dvc, ksteps); break;
-                                default: step_k<6>(vb, dvc, ksteps); break;
-                            }
-#pragma unroll
-                            for (uint32_t c = 0; c < RF_NC; ++c)
-                                if (c < nc) rec[1 + nc + c] = f2u(vb[c]);
-                        }
-                        acc_fi += o.frags_i;
-                        acc_oob += o.oob;
-                        mark_band(band, o, J, word, bit);
-                        __syncwarp();
-                    }
-                    rec_off += (uint32_t)in_rows;
-                    continue;
+                Yh[hh] = Y;
+                inh[hh] = (uint32_t)in_rows;
+            }
+            if (regular) {
+                // Scanlines y: half 0's rows Yh[0] .., then half 1's (the
+                // halves meet at the middle vertex's row), walked in one pass
+                // so a band holding both is visited once.  One lane per row
+                // quantity runs each half's own running sums
+                // (ScanlineIter::next), then one lane per row for the span,
+                // stats and row record (half 1's records follow half 0's).
+                if (lane == 0) {
+                    R->y0 = (uint32_t)Yh[0];
+                    R->c0 = inh[0];
+                    R->y1 = (uint32_t)Yh[1];
+                    R->c1 = inh[1];
                 }
+                const int64_t lo0 = Yh[0], hi0 = Yh[0] + (int64_t)inh[0] - 1;
+                const int64_t lo1 = Yh[1], hi1 = Yh[1] + (int64_t)inh[1] - 1;
+                const int64_t ylo = inh[0] ? lo0 : lo1, yhi = inh[1] ? hi1 : hi0;
+                float wv0 = lane < nr ? u2f(P->half[0].b0[lane]) : 0.0f;
+                const float wd0 = lane < nr ? P->half[0].d[lane] : 0.0f;
+                float wv1 = lane < nr ? u2f(P->half[1].b0[lane]) : 0.0f;
+                const float wd1 = lane < nr ? P->half[1].d[lane] : 0.0f;
+                // Rows a..b of the band starting at row ys from running value wv.
+                auto walk = [&](float &wv, float wd, int64_t a, int64_t b, int64_t ys) {
+                    if (a > b) return;
+                    uint32_t i = (uint32_t)(a - ys);
+                    const uint32_t e = (uint32_t)(b - ys) + 1u;
+                    for (; i + 4u <= e; i += 4u) {  // four rows per trip
+                        const float w1 = fadd(wv, wd), w2 = fadd(w1, wd), w3 = fadd(w2, wd);
+                        T[i][lane] = wv;
+                        T[i + 1][lane] = w1;
+                        T[i + 2][lane] = w2;
+                        T[i + 3][lane] = w3;
+                        wv = fadd(w3, wd);
+                    }
+                    for (; i < e; ++i) {
+                        T[i][lane] = wv;
+                        wv = fadd(wv, wd);
+                    }
+                };
+                for (int64_t band = (inh[0] | inh[1]) ? ylo / RF_TILE_H : 1; band * RF_TILE_H <= yhi; ++band) {
+                    const int64_t ys = max(ylo, band * RF_TILE_H);
+                    const int64_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
+                    if (lane < nr) {
+                        if (inh[0]) walk(wv0, wd0, max(ys, lo0), min(ye, hi0), ys);
+                        if (inh[1]) walk(wv1, wd1, max(ys, lo1), min(ye, hi1), ys);
+                    }
+                    __syncwarp();
+                    const int64_t y = band * RF_TILE_H + lane;
+                    const bool in0 = inh[0] && y >= lo0 && y <= hi0;
+                    const bool in1 = inh[1] && y >= lo1 && y <= hi1;
+                    RowOut o{0, 0, 0xFFFFFFFFu, 0};
+                    if (in0 || in1) {
+                        const uint32_t hh = in0 ? 0u : 1u;
+                        const uint32_t i = (uint32_t)(y - ys);
+                        const uint32_t ridx = in0 ? (uint32_t)(y - lo0) : inh[0] + (uint32_t)(y - lo1);
+                        const float lx = T[i][RF_R_LX], rx = T[i][RF_R_RX];
+                        const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
+                        const uint64_t xs = as_usize_fast(x0r);
+                        uint64_t xe = as_usize_fast(x1r);
+                        if (xe < xs) xe = xs;
+                        o.frags_i = xe - xs;
+                        if (xe > J.w) o.oob = 1;
+                        uint64_t nfr = xe - xs;
+                        const uint32_t cnt = as_u32(fsub(x1r, x0r));
+                        if (cnt < nfr) nfr = cnt;
+                        uint32_t w0 = 0;
+                        if (nfr && xs < J.w) {
+                            o.px0 = (uint32_t)xs;
+                            o.px1 = (uint32_t)(xs + nfr < J.w ? xs + nfr : J.w);
+                            w0 = o.px0 | (o.px1 << 16);
+                        }
+                        uint32_t *rec = rows + base + (size_t)ridx * stride;
+                        rec[0] = w0;
+                        // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102),
+                        // and the varyings at the span's first tile boundary.
+                        const float tshift = fsub(x0r, lx);
+                        const uint32_t kb = w0 ? tile_w - (o.px0 & (tile_w - 1u)) : 0u;
+                        const bool crosses = w0 && o.px0 + kb < o.px1;
+                        const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
+                        // The components step side by side (independent
+                        // chains), each exactly like Iter::next.
+                        const float *dvh = P->half[hh].dvdx;
+                        float vb[RF_NC], dvc[RF_NC];
+#pragma unroll
+                        for (uint32_t c = 0; c < RF_NC; ++c) {
+                            if (c < nc) {
+                                const float cv = T[i][RF_R_C + c];
+                                dvc[c] = dvh[c];
+                                vb[c] = fadd(cv, fmul(fsub(fadd(cv, dvc[c]), cv), tshift));
+                                rec[1 + c] = f2u(vb[c]);
+                            } else {
+                                dvc[c] = 0.0f;
+                                vb[c] = 0.0f;
+                            }
+                        }
+                        switch (nc) {  // only the kind's components step
+                            case 1: step_k<1>(vb, dvc, ksteps); break;
+                            case 2: step_k<2>(vb, dvc, ksteps); break;
+                            case 3: step_k<3>(vb, dvc, ksteps); break;
+                            case 4: step_k<4>(vb, dvc, ksteps); break;
+                            case 5: step_k<5>(vb, dvc, ksteps); break;
+                            default: step_k<6>(vb, dvc, ksteps); break;
+                        }
+#pragma unroll
+                        for (uint32_t c = 0; c < RF_NC; ++c)
+                            if (c < nc) rec[1 + nc + c] = f2u(vb[c]);
+                    }
+                    acc_fi += o.frags_i;
+                    acc_oob += o.oob;
+                    mark_band(band, o, J, word, bit);
+                    __syncwarp();
+                }
+            }
+            for (int hh = 0; hh < 2 && !regular; ++hh) {
+                const HalfRec *H = &P->half[hh];
+                if (inh[hh] == 0) continue;
+                const int64_t Y = Yh[hh];
+                const int64_t in_rows = (int64_t)inh[hh];
                 // Rows above the buffer all land on row 0: walked by lane 0.
                 RowOut o0{0, 0, 0xFFFFFFFFu, 0};
                 int64_t jfirst = 0;
