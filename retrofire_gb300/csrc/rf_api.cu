@@ -585,7 +585,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
     if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
     if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 4))) return st;
-    if ((st = ensure(ctx, ctx->marks, ((size_t)nj + 1) * 8))) return st;
+    if ((st = ensure(ctx, ctx->marks, 8))) return st;
     if ((st = ensure(ctx, ctx->items, (size_t)ntiles * (RF_SPLIT_K + 1) * 4))) return st;
     if (!ctx->rows_need_host) {
         CK(cudaMallocHost(&ctx->rows_need_host, sizeof(unsigned long long)));
@@ -651,7 +651,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(mark(RF_STAGE_VERTEX));
         if (any_cull) CK(rfk::launch_cull(P<DrawDev>(ctx->draws), ndraws, kst, ctx->nsm, s));
         CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
-                              counters, P<unsigned long long>(ctx->marks), nj + 1,
+                              counters, P<unsigned long long>(ctx->marks),
                               ctx->nsm, s));
         CK(mark(RF_STAGE_CLIP));
         CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
@@ -667,7 +667,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                              P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
                              P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
-                             nj, kst, counters, ctx->nsm, s));
+                             kst, counters, ctx->nsm, s));
         CK(rfk::launch_items(jd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
                              (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));
         CK(mark(RF_STAGE_RASTER));
@@ -1038,7 +1038,7 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
         CK(cudaMemsetAsync(counters + RF_CNT_QUEUE, 0, 4, s));
         CK(cudaMemsetAsync(ctx->lmask.p, 0, mwords * 4, s));
         CK(rfk::launch_vertex(P<DrawDev>(ctx->draws), 1, m.nverts, P<float4>(ctx->cpos),
-                              P<uint8_t>(ctx->coc), nullptr, nullptr, 0, ctx->nsm, s));
+                              P<uint8_t>(ctx->coc), nullptr, nullptr, ctx->nsm, s));
         CK(rfk::launch_lines(P<DrawDev>(ctx->draws), P<JobDev>(ctx->jobs), m.ntri, P<float4>(ctx->cpos),
                              P<uint8_t>(ctx->coc), P<LineRec>(ctx->lrec), P<uint32_t>(ctx->lmask), ntiles,
                              counters + RF_CNT_QUEUE, P<StatsDev>(ctx->stats), ctx->nsm, s));

@@ -61,15 +61,14 @@ __device__ __forceinline__ uint32_t zdiv_mask_of(int32_t shader) {
 // ---------------------------------------------------------------------------
 __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t nv_total,
                          float4 *__restrict__ cpos, uint8_t *__restrict__ coc,
-                         uint32_t *__restrict__ counters, unsigned long long *__restrict__ jmarks,
-                         uint32_t njm) {
+                         uint32_t *__restrict__ counters, unsigned long long *__restrict__ marks) {
     if (blockIdx.x == 0) {  // the frame's counters, for the kernels after this one
         if (counters && threadIdx.x == 0) {
             counters[RF_CNT_POOL] = 0;
             counters[RF_CNT_QUEUE] = 0;
             counters[RF_CNT_LIVE] = 0;
+            *marks = 0;
         }
-        for (uint32_t j = threadIdx.x; j < njm; j += blockDim.x) jmarks[j] = 0;
     }
     // Warp-uniform loop (the draw lookup is shared by the warp's lanes).
     for (uint32_t wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wbase < nv_total;
@@ -748,7 +747,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
       const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
       unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
       StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
-      unsigned long long *__restrict__ jmarks, uint32_t nj) {
+      unsigned long long *__restrict__ marks) {
     const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -783,16 +782,12 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     uint32_t cur_job = 0xFFFFFFFFu;
     unsigned long long acc_fi = 0, acc_oob = 0;  // per-lane, for cur_job
     uint32_t acc_marks = 0;                        // (triangle, tile) bits set by this lane
-    unsigned long long all_marks = 0;  // every job's, for the frame total
     auto flush = [&]() {
         if (cur_job != 0xFFFFFFFFu) {
             warp_add_u64(&stats[cur_job].frags_i, acc_fi, true);
             warp_add_u64(&stats[cur_job].oob, acc_oob, true);
-            warp_add_u64(&jmarks[cur_job], acc_marks, true);
         }
-        all_marks += acc_marks;
         acc_fi = acc_oob = 0;
-        acc_marks = 0;
     };
     // One band of the target: reduce the lanes' covered columns and mark the
     // band's tiles with this triangle's bit.
@@ -1055,7 +1050,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         }
     }
     flush();
-    warp_add_u64(&jmarks[nj], all_marks, true);
+    warp_add_u64(marks, acc_marks, true);
 }
 
 // The rasteriser's work list.  A tile walks its triangles serially, so the
@@ -1071,15 +1066,15 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
 // k_tile_items: one warp per tile.  Its nonzero mask words (the set bits
 // of its summary words) stand for its triangle count: at most the count,
 // about it where the tile's triangles are scattered through the submission
-// order.  A crowded tile is one whose nonzero words alone exceed four times
-// its scene's mean (marks / tiles: an outlier of its own scene) and the
-// frame's marks per resident warp (its walk alone outlasts a warp's fair
-// share of the pass, so splitting it shortens the pass).
+// order; where most words are nonzero the bits are counted instead.  A
+// crowded tile is one whose count exceeds twice the frame's marks per
+// resident warp: its walk alone would outlast two warps' fair shares of
+// the pass, so splitting it shortens the pass.
 #define RF_SPLIT_MIN 64u  // a tile with fewer binned triangles is never split
 #define RF_HEAVY_MIN 16u  // ... nor taken early
 __global__ void __launch_bounds__(256)
 k_tile_items(const JobDev *__restrict__ jobs, uint32_t nj, const uint32_t *__restrict__ mask,
-             uint32_t ntiles, const unsigned long long *__restrict__ jmarks, uint32_t slots,
+             uint32_t ntiles, const unsigned long long *__restrict__ marks, uint32_t slots,
              uint32_t *__restrict__ items, uint32_t *__restrict__ extra) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1091,14 +1086,20 @@ k_tile_items(const JobDev *__restrict__ jobs, uint32_t nj, const uint32_t *__res
     uint32_t c = 0;
     for (uint32_t i = lane; i < J.sum_words; i += 32) c += __popc(sw[i]);
     c = __reduce_add_sync(0xFFFFFFFFu, c);
+    if (2u * c >= J.mask_words) {
+        // Half the mask words or more are nonzero: they say little about
+        // the count, so count the bits (a few small busy scenes do this).
+        const uint32_t *mw = mask + J.mask_base + (size_t)lt * J.mask_words;
+        c = 0;
+        for (uint32_t i = lane; i < J.mask_words; i += 32) c += __popc(mw[i]);
+        c = __reduce_add_sync(0xFFFFFFFFu, c);
+    }
     if (lane == 0) {
-        const unsigned long long mean4 = 4ull * jmarks[ji] / ((unsigned long long)J.tiles_x * J.tiles_y);
-        const unsigned long long share = jmarks[nj] / slots;
-        const uint32_t thr =
-            (uint32_t)min(max(max((unsigned long long)RF_SPLIT_MIN, mean4), share), 0xFFFFFFFFull);
+        const unsigned long long share2 = 2ull * *marks / slots;
+        const uint32_t thr = (uint32_t)min(max((unsigned long long)RF_SPLIT_MIN, share2), 0xFFFFFFFFull);
         const bool crowded = c > thr;
         // Heavy: more than twice the frame's mean; taken before the rest.
-        const bool heavy = crowded || (c > RF_HEAVY_MIN && c > 2ull * jmarks[nj] / ntiles);
+        const bool heavy = crowded || (c > RF_HEAVY_MIN && c > 2ull * *marks / ntiles);
         items[tile] = heavy ? RF_ITEM_SKIP : tile * 8u;
         if (crowded) {
             const uint32_t at = ntiles + atomicAdd(extra, RF_SPLIT_K);
@@ -1125,11 +1126,11 @@ __global__ void k_fill(uint32_t *__restrict__ color, float *__restrict__ depth, 
 namespace rfk {
 
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
-                          uint8_t *coc, uint32_t *counters, unsigned long long *jmarks, uint32_t njm,
+                          uint8_t *coc, uint32_t *counters, unsigned long long *marks,
                           int nsm, cudaStream_t s) {
     if (nv == 0) return cudaSuccess;
     uint32_t blocks = min((nv + 255) / 256, (uint32_t)nsm * 16);
-    k_vertex<<<blocks, 256, 0, s>>>(draws, nd, nv, cpos, coc, counters, jmarks, njm);
+    k_vertex<<<blocks, 256, 0, s>>>(draws, nd, nv, cpos, coc, counters, marks);
     return cudaGetLastError();
 }
 
@@ -1168,8 +1169,8 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *jmarks,
-                         uint32_t nj, StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s) {
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
+                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s) {
     cudaError_t e;
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
@@ -1192,16 +1193,16 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     // one warp per live output triangle; the count is only known on the device
     uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
     k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap,
-                                  rprims, mask, stats, counters, jmarks, nj);
+                                  rprims, mask, stats, counters, marks);
     return cudaGetLastError();
 }
 
 cudaError_t launch_items(const JobDev *jobs, uint32_t nj, const uint32_t *mask, uint32_t ntiles,
-                         const unsigned long long *jmarks, uint32_t slots, uint32_t *items,
+                         const unsigned long long *marks, uint32_t slots, uint32_t *items,
                          uint32_t *counters, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     k_tile_items<<<(uint32_t)(((uint64_t)ntiles * 32 + 255) / 256), 256, 0, s>>>(
-        jobs, nj, mask, ntiles, jmarks, slots ? slots : 1u, items, counters + RF_CNT_ITEMS);
+        jobs, nj, mask, ntiles, marks, slots ? slots : 1u, items, counters + RF_CNT_ITEMS);
     return cudaGetLastError();
 }
 

@@ -52,9 +52,9 @@
 
 namespace rfk {
 // counters (optional): POOL, QUEUE and LIVE zeroed for the kernels after
-// it, and jmarks[0 .. njm) (the binning pass's per-scene marks).
+// it, and *marks (the binning pass's total of (triangle, tile) bits).
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
-                          uint8_t *coc, uint32_t *counters, unsigned long long *jmarks, uint32_t njm,
+                          uint8_t *coc, uint32_t *counters, unsigned long long *marks,
                           int nsm, cudaStream_t s);
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
                         const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, PolyVert *pool,
@@ -67,8 +67,8 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 // u64) and scan64 (scan64_scratch_words(nt) u64) are scratch; rows holds
 // rows_cap words; rows_total receives the words the frame asked for; live
 // (room for every output triangle) receives the indices of the triangles
-// that pass the face-cull test, counters[RF_CNT_LIVE] their number; jmarks
-// (nj + 1) receives each scene's (triangle, tile) bits, then their sum.
+// that pass the face-cull test, counters[RF_CNT_LIVE] their number; *marks
+// receives the (triangle, tile) bits set in all.
 size_t scan64_scratch_words(uint32_t n);
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
@@ -76,9 +76,9 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *jmarks,
-                         uint32_t nj, StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s);
-// The rasteriser's work list from the tile masks and the scenes' marks
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
+                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s);
+// The rasteriser's work list from the tile masks and the marks total
 // (slots: the warps the rasteriser keeps resident, about).  items (room
 // for (RF_SPLIT_K + 1) * ntiles): items[ntiles .. ntiles + extra) first --
 // heavy tiles (tile * 8) and the row slices of crowded tiles (tile * 8 + k,
@@ -86,7 +86,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
 // order, RF_ITEM_SKIP for the tiles already listed; extra is
 // counters[RF_CNT_ITEMS] (zeroed by launch_setup).
 cudaError_t launch_items(const JobDev *jobs, uint32_t nj, const uint32_t *mask, uint32_t ntiles,
-                         const unsigned long long *jmarks, uint32_t slots, uint32_t *items,
+                         const unsigned long long *marks, uint32_t slots, uint32_t *items,
                          uint32_t *counters, cudaStream_t s);
 #define RF_SPLIT_K 4  // row slices of a crowded tile (RF_TILE_H / RF_SPLIT_K rows each)
 #define RF_ITEM_SKIP 0xFFFFFFFEu  // a work-list entry taken elsewhere in the list

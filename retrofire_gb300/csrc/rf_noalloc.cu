@@ -231,13 +231,13 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
         NA_CK(cudaMemcpyAsync(dd, &d, sizeof d, cudaMemcpyHostToDevice, s));
         NA_CK(cudaMemcpyAsync(jd, &J, sizeof J, cudaMemcpyHostToDevice, s));
         NA_CK(cudaMemsetAsync(mask, 0, (size_t)ntiles * (J.mask_words + J.sum_words) * 4, s));
-        NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, cnt, marks, 2, nsm, s));
+        NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, cnt, marks, nsm, s));
         NA_CK(rfk::launch_clip(dd, 1, ntri, cpos, coc, tcnt, tpoly, pool, RF_NOALLOC_MAX_TRIS,
                                cnt, nsm, s));
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
                                 triw, trib, scan64, rowtot, rows, ROWS_WORDS, rprims, mask, live,
-                                marks, 1, sd, cnt, nsm, s));
+                                marks, sd, cnt, nsm, s));
         NA_CK(rfk::launch_items(jd, 1, mask, ntiles, marks, (uint32_t)nsm * 16u, items, cnt, s));
         const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
                           flags->depth_write;
