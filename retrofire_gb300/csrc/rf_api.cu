@@ -655,7 +655,8 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                               ctx->nsm, s));
         CK(mark(RF_STAGE_CLIP));
         CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
-                            P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
+                            P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<uint32_t>(ctx->toff),
+                            P<PolyVert>(ctx->pool),
                             pool_cap, counters, ctx->nsm, s));
         CK(mark(RF_STAGE_SCAN));
         CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
@@ -725,9 +726,9 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(cudaEventRecord(tuned->e1, s));
         tuned->pending = true;
     }
-    // vertex, clip, scan (3, or 1 for one block), setup, scan64 (the same), bin,
-    // work list, raster (+ the stats fold)
-    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 8 : 12) + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
+    // vertex, clip (2), scan (3, or 1 for one block), setup, scan64 (the same),
+    // bin, work list, raster (+ the stats fold)
+    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 9 : 13) + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));

@@ -67,6 +67,7 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
             counters[RF_CNT_POOL] = 0;
             counters[RF_CNT_QUEUE] = 0;
             counters[RF_CNT_LIVE] = 0;
+            counters[RF_CNT_CLIPQ] = 0;
             *marks = 0;
         }
     }
@@ -167,10 +168,12 @@ __device__ int clip_plane(int plane, const CV *in, int nin, CV *out, uint32_t na
 }
 }  // namespace
 
+// Classification (clip.rs:245-267 status): one thread per triangle; the
+// few that cross a plane go to a queue for k_clip_poly, so the clipping
+// loop runs on full warps.
 __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t nt_total,
-                       const float4 *__restrict__ cpos, const uint8_t *__restrict__ coc,
-                       uint32_t *__restrict__ tcnt, uint32_t *__restrict__ tpoly,
-                       PolyVert *__restrict__ pool, uint32_t pool_cap,
+                       const uint8_t *__restrict__ coc, uint32_t *__restrict__ tcnt,
+                       uint32_t *__restrict__ tpoly, uint32_t *__restrict__ queue,
                        uint32_t *__restrict__ counters) {
     // Warp-uniform loop (the draw lookup is shared by the warp's lanes).
     for (uint32_t wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wbase < nt_total;
@@ -178,78 +181,101 @@ __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t 
         const uint32_t gt = wbase + (threadIdx.x & 31u);
         const uint32_t di = warp_upper_index(nd, gt < nt_total ? gt : nt_total - 1,
                                              [&](uint32_t i) { return draws[i].tri_base; });
-        if (gt >= nt_total) continue;
-        const DrawDev &d = draws[di];
-        if (d.culled) {  // a render() call that is not made: no output
-            tcnt[gt] = 0;
-            tpoly[gt] = RF_NO_POLY;
-            continue;
-        }
-        const uint32_t t = gt - d.tri_base;
-        uint32_t vi[3], oc[3];
-        bool bad = false;
+        bool clipped = false;
+        if (gt < nt_total) {
+            const DrawDev &d = draws[di];
+            uint32_t cnt = 0;
+            if (!d.culled) {  // (a culled draw is a render() call that is not made: no output)
+                const uint32_t t = gt - d.tri_base;
+                uint32_t vi[3];
+                bool bad = false;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            vi[k] = d.idx[3 * (size_t)t + k];
-            bad |= vi[k] >= d.nverts;
-            vi[k] = bad ? 0u : vi[k] + d.vert_base;
-        }
-        uint32_t cnt = 0, slot = RF_NO_POLY;
-        if (bad) {
-            atomicAdd(&counters[RF_CNT_BADIDX], 1u);  // index out of range (render.rs:170 panics)
-        } else {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) oc[k] = coc[vi[k]];
-            if ((oc[0] & oc[1] & oc[2]) != 0u) {
-                cnt = 0;  // Hidden
-            } else if ((oc[0] | oc[1] | oc[2]) == 0u) {
-                cnt = 1;  // Visible
-            } else {
-                CV A[RF_POLY_CAP], B[RF_POLY_CAP];
-                const uint32_t na = d.nattr < RF_MAX_ATTR ? d.nattr : RF_MAX_ATTR;
                 for (int k = 0; k < 3; ++k) {
-                    const float4 p = cpos[vi[k]];
-                    A[k].pos[0] = p.x; A[k].pos[1] = p.y; A[k].pos[2] = p.z; A[k].pos[3] = p.w;
-                    const float *src = d.verts + (size_t)(vi[k] - d.vert_base) * d.stride + d.pos_dim;
-                    for (uint32_t c = 0; c < na; ++c) A[k].a[c] = src[c];
-                    A[k].oc = oc[k];
+                    vi[k] = d.idx[3 * (size_t)t + k];
+                    bad |= vi[k] >= d.nverts;
                 }
-                CV *vin = A, *vout = B;
-                int nin = 3, nout = 0;
-                bool ovf = false;
-                for (int pl = 0; pl < 6; ++pl) {
-                    nout = clip_plane(pl, vin, nin, vout, na, ovf);
-                    nin = 0;
-                    if (nout == 0) break;
-                    if (pl < 5) {
-                        CV *tmp = vin; vin = vout; vout = tmp;
-                        nin = nout; nout = 0;
-                    }
+                if (bad) {
+                    atomicAdd(&counters[RF_CNT_BADIDX], 1u);  // index out of range (render.rs:170 panics)
+                } else {
+                    const uint32_t o0 = coc[vi[0] + d.vert_base], o1 = coc[vi[1] + d.vert_base],
+                                   o2 = coc[vi[2] + d.vert_base];
+                    if ((o0 & o1 & o2) != 0u) cnt = 0;       // Hidden
+                    else if ((o0 | o1 | o2) == 0u) cnt = 1;  // Visible
+                    else clipped = true;
                 }
-                if (nout > RF_POLY_STORE) ovf = true;
-                if (ovf) {
-                    // Only reachable through float pathologies (a convex
-                    // triangle gains at most one vertex per plane); counted
-                    // in stats.oob and dropped.
-                    atomicAdd(&counters[RF_CNT_POLYOVF], 1u);
-                    nout = 0;
-                }
-                cnt = nout >= 3 ? (uint32_t)(nout - 2) : 0u;
-                if (cnt) {
-                    slot = atomicAdd(&counters[RF_CNT_POOL], 1u);
-                    if (slot < pool_cap) {
-                        PolyVert *dst = pool + (size_t)slot * RF_POLY_STORE;
-                        for (int k = 0; k < nout; ++k) {
+            }
+            tcnt[gt] = cnt;
+            tpoly[gt] = clipped ? di : RF_NO_POLY;  // (a queued triangle's draw, for k_clip_poly)
+        }
+        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, clipped);
+        if (bal) {
+            const uint32_t lane = threadIdx.x & 31u, lead = __ffs(bal) - 1;
+            uint32_t at = 0;
+            if (lane == lead) at = atomicAdd(&counters[RF_CNT_CLIPQ], (uint32_t)__popc(bal));
+            at = __shfl_sync(0xFFFFFFFFu, at, lead);
+            if (clipped) queue[at + __popc(bal & ((1u << lane) - 1u))] = gt;
+        }
+    }
+}
+
+// Sutherland-Hodgman for the queued triangles (clip.rs:283-301, 350-400),
+// one thread each; the polygon goes to a pool slot, its fan count to tcnt.
+__global__ void k_clip_poly(const DrawDev *__restrict__ draws,
+                            const float4 *__restrict__ cpos, const uint8_t *__restrict__ coc,
+                            uint32_t *__restrict__ tcnt, uint32_t *__restrict__ tpoly,
+                            const uint32_t *__restrict__ queue, PolyVert *__restrict__ pool,
+                            uint32_t pool_cap, uint32_t *__restrict__ counters) {
+    const uint32_t nq = counters[RF_CNT_CLIPQ];
+    for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
+        const uint32_t gt = queue[qi];
+        const DrawDev &d = draws[tpoly[gt]];  // k_clip left the draw index there
+        const uint32_t t = gt - d.tri_base;
+        uint32_t vi[3];
 #pragma unroll
-                            for (int c = 0; c < 4; ++c) dst[k].pos[c] = vout[k].pos[c];
-                            for (uint32_t c = 0; c < na; ++c) dst[k].a[c] = vout[k].a[c];
-                        }
-                    } else {
-                        atomicAdd(&counters[RF_CNT_POOLOVF], 1u);
-                        cnt = 0;
-                        slot = RF_NO_POLY;
-                    }
+        for (int k = 0; k < 3; ++k) vi[k] = d.idx[3 * (size_t)t + k] + d.vert_base;
+        CV A[RF_POLY_CAP], B[RF_POLY_CAP];
+        const uint32_t na = d.nattr < RF_MAX_ATTR ? d.nattr : RF_MAX_ATTR;
+        for (int k = 0; k < 3; ++k) {
+            const float4 p = cpos[vi[k]];
+            A[k].pos[0] = p.x; A[k].pos[1] = p.y; A[k].pos[2] = p.z; A[k].pos[3] = p.w;
+            const float *src = d.verts + (size_t)(vi[k] - d.vert_base) * d.stride + d.pos_dim;
+            for (uint32_t c = 0; c < na; ++c) A[k].a[c] = src[c];
+            A[k].oc = coc[vi[k]];
+        }
+        CV *vin = A, *vout = B;
+        int nin = 3, nout = 0;
+        bool ovf = false;
+        for (int pl = 0; pl < 6; ++pl) {
+            nout = clip_plane(pl, vin, nin, vout, na, ovf);
+            nin = 0;
+            if (nout == 0) break;
+            if (pl < 5) {
+                CV *tmp = vin; vin = vout; vout = tmp;
+                nin = nout; nout = 0;
+            }
+        }
+        if (nout > RF_POLY_STORE) ovf = true;
+        if (ovf) {
+            // Only reachable through float pathologies (a convex triangle
+            // gains at most one vertex per plane); counted in stats.oob and
+            // dropped.
+            atomicAdd(&counters[RF_CNT_POLYOVF], 1u);
+            nout = 0;
+        }
+        uint32_t cnt = nout >= 3 ? (uint32_t)(nout - 2) : 0u, slot = RF_NO_POLY;
+        if (cnt) {
+            slot = atomicAdd(&counters[RF_CNT_POOL], 1u);
+            if (slot < pool_cap) {
+                PolyVert *dst = pool + (size_t)slot * RF_POLY_STORE;
+                for (int k = 0; k < nout; ++k) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) dst[k].pos[c] = vout[k].pos[c];
+                    for (uint32_t c = 0; c < na; ++c) dst[k].a[c] = vout[k].a[c];
                 }
+            } else {
+                atomicAdd(&counters[RF_CNT_POOLOVF], 1u);
+                cnt = 0;
+                slot = RF_NO_POLY;
             }
         }
         tcnt[gt] = cnt;
@@ -1135,11 +1161,15 @@ cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4
 }
 
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
-                        const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, PolyVert *pool,
-                        uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s) {
+                        const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, uint32_t *queue,
+                        PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s) {
     if (nt == 0) return cudaSuccess;
-    uint32_t blocks = min((nt + 127) / 128, (uint32_t)nsm * 16);
-    k_clip<<<blocks, 128, 0, s>>>(draws, nd, nt, cpos, coc, tcnt, tpoly, pool, pool_cap, counters);
+    const uint32_t blocks = min((nt + 255) / 256, (uint32_t)nsm * 16);
+    k_clip<<<blocks, 256, 0, s>>>(draws, nd, nt, coc, tcnt, tpoly, queue, counters);
+    // The queue's length is known on the device only: a grid for all of it
+    // at the worst case, each thread striding over what is there.
+    const uint32_t pblocks = min((nt + 127) / 128, (uint32_t)nsm * 4);
+    k_clip_poly<<<pblocks, 128, 0, s>>>(draws, cpos, coc, tcnt, tpoly, queue, pool, pool_cap, counters);
     return cudaGetLastError();
 }
 

@@ -47,18 +47,21 @@
 #define RF_CNT_ROWSOVF 6  // triangles rasterised without row records (buffer full)
 #define RF_CNT_LIVE 7     // output triangles that passed the face-cull test
 #define RF_CNT_ITEMS 8    // rasteriser work items after the first ntiles (slices of crowded tiles)
+#define RF_CNT_CLIPQ 10   // triangles queued for clipping
 #define RF_CNT_N 16
 #define RF_SCAN_BLOCK_ITEMS 4096u  // values one scan block takes (one launch instead of three)
 
 namespace rfk {
-// counters (optional): POOL, QUEUE and LIVE zeroed for the kernels after
+// counters (optional): POOL, QUEUE, LIVE and CLIPQ zeroed for the kernels after
 // it, and *marks (the binning pass's total of (triangle, tile) bits).
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
                           uint8_t *coc, uint32_t *counters, unsigned long long *marks,
                           int nsm, cudaStream_t s);
+// queue: room for nt triangle indices (scratch until the scan: the caller
+// passes the scan's output array).
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
-                        const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, PolyVert *pool,
-                        uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s);
+                        const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, uint32_t *queue,
+                        PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s);
 size_t scan_scratch_words(uint32_t n);
 cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch,
                         uint32_t *total, cudaStream_t s);

@@ -231,7 +231,7 @@ def test_graph_replay_same_shape():
         cnt = dev.counts()
         assert cnt["graphs_cached"] == 1
         assert cnt["graph_launches"] == 6
-        assert cnt["kernels"] == 6 * 8  # eight kernels per frame (one-block scans)
+        assert cnt["kernels"] == 6 * 9  # nine kernels per frame (one-block scans)
     finally:
         dev.close()
 
