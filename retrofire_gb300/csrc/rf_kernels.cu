@@ -1,16 +1,19 @@
 // rf_kernels.cu — CUDA kernels of the triangle render path (sm_103a).
 //
 // Stage map (reference call stack: core/src/render.rs:134-207):
-//   k_vertex   vertex shader + ClipVert::new         render.rs:157-165
-//   k_clip     status + Sutherland-Hodgman count      clip.rs:245-301,350-400
-//   k_scan_*   order-preserving compaction offsets    (submission order)
-//   k_setup    to_screen, face cull, tri_fill/scan    prim.rs:62-88, raster.rs:185-302
-//              setup
-//   k_bin      scanline stats (frags.i, oob) and      raster.rs:80-114, target.rs:259-264
-//              tile binning, one warp per triangle
-//   k_raster   per-tile scan conversion, depth test,  raster.rs:80-114, target.rs:163-198
-//              fragment shading, pixel packing
-//   k_fill     Frame::clear without a later render    front/src/lib.rs:103-120
+//   k_vertex     vertex shader + ClipVert::new         render.rs:157-165
+//   k_clip       status; the crossing triangles queue  clip.rs:245-267
+//   k_clip_poly  Sutherland-Hodgman on the queue       clip.rs:283-301,350-400
+//   k_scan_*     order-preserving compaction offsets   (submission order)
+//   k_setup      to_screen, face cull, tri_fill/scan   prim.rs:62-88, raster.rs:185-302
+//                setup, the live list
+//   k_bin        scanline walk: stats (frags.i, oob),  raster.rs:80-114, target.rs:259-264
+//                row records, tile binning, one warp
+//                per live triangle
+//   k_tile_items the rasteriser's work list            (scheduling only)
+//   k_raster     per-tile span fill, depth test,       raster.rs:60-69, target.rs:163-198
+//                fragment shading, pixel packing       (rf_raster.cuh)
+//   k_fill       Frame::clear without a later render   front/src/lib.rs:103-120
 #include <cuda_runtime.h>
 
 #include "rf_exact.cuh"

@@ -15,9 +15,14 @@
 // order in which the lane walks the triangle list — no atomics, no sorting.
 // Colour and depth sit in shared memory column-major (word x*32 + r): the
 // bank of every access is the lane id, whatever x each lane is at.
-// Each lane enters its row with exact jump-aheads (rfx::seq_add_n) from the
-// triangle setup: the scanline's edge values after j rows, then the span's
-// varyings after k pixels, then steps pixel by pixel like Iter::next.
+// Each lane reads its row's record (written by the binning pass from the
+// reference's own running sums: the clipped span, the varyings at its first
+// fragment and at its first tile boundary), enters the tile from one of
+// those -- or, in a third or later tile of a long span, with an exact jump
+// (rfx::jump) of whole tile widths from the boundary values -- then steps
+// pixel by pixel like Iter::next.  Warps take work items (a tile, or a row
+// slice of a crowded one) from the list k_tile_items builds; triangle
+// headers and row records come in through cp.async rings in shared memory.
 // ---------------------------------------------------------------------------
 namespace rfr {
 using namespace rfx;
