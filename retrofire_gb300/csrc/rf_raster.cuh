@@ -500,101 +500,179 @@ __device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restric
     }
 }
 
+// Warp-wide selection of set bits in order: lane L offers the bits b (lane
+// order, then bit order within a word); the first `want` of them go to the
+// output slots first, first + 1, ...  Lane first + k learns where its bit
+// came from (src lane, bit pos).  take = how many were handed out, total =
+// how many were offered; end_lane / end_rest: the lane of the last bit taken
+// and its bits still left.
+struct WarpTake {
+    uint32_t take, total, src, pos, end_lane, end_rest;
+};
+// Position of the r-th set bit of v (r >= 1, at most popc(v)): halving
+// search on popcounts.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t v, uint32_t r) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 16; w >= 1; w >>= 1) {
+        const uint32_t c = __popc(v & ((1u << w) - 1u));
+        if (c < r) {
+            r -= c;
+            v >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+// (Out of line: it runs once per 32 triangles, and the kernels that switch
+// on the shader kind per triangle are large already.)
+static __device__ __noinline__ WarpTake warp_take(uint32_t b, uint32_t want, uint32_t first, uint32_t lane) {
+    WarpTake t;
+    const uint32_t c = __popc(b);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    t.total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    t.take = min(want, t.total);
+    // Slot k = lane - first comes from the first lane whose inclusive count
+    // exceeds k.
+    const uint32_t k = lane - first;  // huge for lane < first: ignored
+    uint32_t L = 0;
+#pragma unroll
+    for (uint32_t step = 16; step >= 1; step >>= 1) {
+        const uint32_t v = __shfl_sync(0xFFFFFFFFu, incl, L + step - 1);
+        if (v <= k) L += step;
+    }
+    const uint32_t ex = incl - c;
+    const uint32_t exL = __shfl_sync(0xFFFFFFFFu, ex, L);
+    const uint32_t bL = __shfl_sync(0xFFFFFFFFu, b, L);
+    t.src = L;
+    t.pos = nth_set_bit(bL, k - exL + 1u);  // (meaningless on lanes outside the take)
+    // Where the take stopped: the source of slot take - 1.
+    const uint32_t last = first + (t.take ? t.take : 1u) - 1u;
+    t.end_lane = __shfl_sync(0xFFFFFFFFu, L, last & 31u);
+    const uint32_t end_ex = __shfl_sync(0xFFFFFFFFu, exL, last & 31u);
+    const uint32_t end_b = __shfl_sync(0xFFFFFFFFu, bL, last & 31u);
+    const uint32_t used = t.take - end_ex;  // bits of end_lane taken
+    const uint32_t lastpos = nth_set_bit(end_b, used ? used : 1u);
+    t.end_rest = used ? (end_b & ~((2u << lastpos) - 1u)) : end_b;
+    return t;
+}
+
 // Walks a tile's bitmask in submission order: set bits of the mask words
 // (input triangles), each expanded to its clipped output triangles.  The
 // tile's summary words (one bit per nonzero mask word) are read 128 at a
 // time; the nonzero mask words they name are then fetched 32 at a time
 // (lane e loads entry e), so an empty stretch of the mask costs nothing.
-// The next 32 input triangles are gathered at once, lane k holding the
-// k-th one's output range (toff, tcnt loaded in parallel), so one load
-// latency covers 32 triangles.  Warp-uniform state; every lane calls
-// next() together.
+// Both gathers pick their next 32 set bits with one warp-wide prefix count
+// (warp_take), not bit by bit.  The next 32 input triangles are gathered at
+// once, lane k holding the k-th one's output range (toff, tcnt loaded in
+// parallel), so one load latency covers 32 triangles.  Warp-uniform state;
+// every lane calls next() together.
 struct PrimIter {
     const uint32_t *tmask;  // the tile's mask words
     const uint32_t *tsum;   // the tile's summary words
     const uint32_t *toff;
     const uint32_t *tcnt;
     uint32_t nsum, tri_base, lane;
-    // Summary words: lane L holds words sb + 32 c + L, c = 0..3.
-    uint32_t sb, s1, s2, s3, sword, schunk, sbal, ssrc, sv;
-    // Gathered mask words: lane e holds entry e (index widx, value wval).
-    uint32_t widx, wval, wn, wi;
-    uint32_t cur, curw;  // bits left of the current mask word, its index
+    // Summary words, 128 at a time: lane L holds words sb + 32 c + L in
+    // s[c]; the cursor is chunk sc, lane sl, and srem = the bits of that
+    // lane's word not taken yet (words of lower lanes are taken).
+    uint32_t sb, s0, s1, s2, s3, sc, sl, srem;
+    // Gathered mask words: lane e holds entry e (index widx, value wval),
+    // wn of them; the cursor is entry wi with wrem = its bits not taken yet.
+    uint32_t widx, wval, wn, wi, wrem;
     uint32_t p, pend;
     uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
     uint32_t keep;                // entries of the batch to walk
     const RasterPrim *rprims;
     uint32_t slo, shi;            // rows of a row-slice item (slo >= shi: the whole tile)
-    bool started;
-    // Index of the next nonzero mask word, or false.
-    __device__ __forceinline__ bool next_word(uint32_t &w) {
-        for (;;) {
-            if (sv) {
-                const uint32_t b = __ffs(sv) - 1;
-                sv &= sv - 1;
-                w = (sb + schunk * 32 + ssrc) * 32 + b;
-                return true;
-            }
-            if (sbal) {
-                ssrc = __ffs(sbal) - 1;
-                sbal &= sbal - 1;
-                sv = __shfl_sync(0xFFFFFFFFu, sword, ssrc);
-                continue;
-            }
-            if (started && schunk < 3) {
-                ++schunk;
-                sword = schunk == 1 ? s1 : (schunk == 2 ? s2 : s3);
-                sbal = __ballot_sync(0xFFFFFFFFu, sword != 0u);
-                continue;
-            }
-            if (started) sb += 128;
-            started = true;
-            if (sb >= nsum) return false;
-            const uint32_t i0 = sb + lane;
-            sword = i0 < nsum ? tsum[i0] : 0u;
-            s1 = i0 + 32 < nsum ? tsum[i0 + 32] : 0u;
-            s2 = i0 + 64 < nsum ? tsum[i0 + 64] : 0u;
-            s3 = i0 + 96 < nsum ? tsum[i0 + 96] : 0u;
-            schunk = 0;
-            sbal = __ballot_sync(0xFFFFFFFFu, sword != 0u);
-        }
+    bool started, done;           // a window was loaded; the summary words are all read
+
+    __device__ __forceinline__ uint32_t chunk_word() const {
+        return sc == 0 ? s0 : (sc == 1 ? s1 : (sc == 2 ? s2 : s3));
     }
-    __device__ __forceinline__ void word_refill() {
-        uint32_t mine = 0, n = 0, w;
-        while (n < 32u && next_word(w)) {
-            if (lane == n) mine = w;
-            ++n;
+    // The next up to 32 nonzero mask words, in order, into the word batch.
+    __device__ __forceinline__ void gather_words() {
+        uint32_t n = 0, mine = 0;
+        for (;;) {
+            if (!started || sc == 4) {  // next window of summary words
+                if (started) sb += 128;
+                started = true;
+                if (sb >= nsum) {
+                    done = true;
+                    break;
+                }
+                const uint32_t i0 = sb + lane;
+                s0 = i0 < nsum ? tsum[i0] : 0u;
+                s1 = i0 + 32 < nsum ? tsum[i0 + 32] : 0u;
+                s2 = i0 + 64 < nsum ? tsum[i0 + 64] : 0u;
+                s3 = i0 + 96 < nsum ? tsum[i0 + 96] : 0u;
+                sc = 0;
+                sl = 0;
+                srem = __shfl_sync(0xFFFFFFFFu, s0, 0);
+            }
+            const uint32_t w = chunk_word();
+            const uint32_t b = lane < sl ? 0u : (lane == sl ? srem : w);
+            if (__ballot_sync(0xFFFFFFFFu, b != 0u) == 0u) {  // nothing left in this chunk
+                if (++sc < 4) {
+                    sl = 0;
+                    srem = __shfl_sync(0xFFFFFFFFu, chunk_word(), 0);
+                }
+                continue;
+            }
+            WarpTake t = warp_take(b, 32u - n, n, lane);
+            if (lane >= n && lane < n + t.take) mine = (sb + sc * 32u + t.src) * 32u + t.pos;
+            n += t.take;
+            if (t.take < t.total) {  // stopped inside this chunk
+                sl = t.end_lane;
+                srem = t.end_rest;
+                break;
+            }
+            ++sc;  // chunk used up
+            if (sc < 4) {
+                sl = 0;
+                srem = __shfl_sync(0xFFFFFFFFu, chunk_word(), 0);
+            }
+            if (n == 32u) break;
         }
         wn = n;
         wi = 0;
         widx = mine;
         wval = lane < n ? tmask[mine] : 0u;
+        wrem = __shfl_sync(0xFFFFFFFFu, wval, 0);
     }
-    // Next set bit (input triangle, global index) or false.
-    __device__ __forceinline__ bool next_bit(uint32_t &gt) {
-        for (;;) {
-            if (cur) {
-                const uint32_t b = __ffs(cur) - 1;
-                cur &= cur - 1;
-                gt = tri_base + curw * 32 + b;
-                return true;
+    // The next up to 32 input triangles (set bits), in order: lane k holds
+    // the k-th one's global index in mine; returns how many.
+    __device__ __forceinline__ uint32_t gather_tris(uint32_t &mine) {
+        uint32_t n = 0;
+        mine = 0;
+        while (n < 32u) {
+            if (wi >= wn) {
+                if (done) break;  // no summary words left
+                gather_words();
+                if (wn == 0) break;
             }
-            if (wi < wn) {
-                cur = __shfl_sync(0xFFFFFFFFu, wval, wi);
-                curw = __shfl_sync(0xFFFFFFFFu, widx, wi);
-                ++wi;
-                continue;
+            const uint32_t b = (lane < wi || lane >= wn) ? 0u : (lane == wi ? wrem : wval);
+            WarpTake t = warp_take(b, 32u - n, n, lane);
+            const uint32_t wsrc = __shfl_sync(0xFFFFFFFFu, widx, t.src);
+            if (lane >= n && lane < n + t.take) mine = tri_base + wsrc * 32u + t.pos;
+            n += t.take;
+            if (t.take < t.total) {  // stopped inside this word batch
+                wi = t.end_lane;
+                wrem = t.end_rest;
+            } else {
+                wi = wn;  // batch used up
             }
-            word_refill();
-            if (wn == 0) return false;
         }
+        return n;
     }
     __device__ __forceinline__ void refill() {
-        uint32_t mine = 0, n = 0, gt;
-        while (n < 32u && next_bit(gt)) {
-            if (lane == n) mine = gt;
-            ++n;
-        }
+        uint32_t mine;
+        const uint32_t n = gather_tris(mine);
         bn = n;
         bi = 0;
         bool take = lane < n;
@@ -615,10 +693,10 @@ struct PrimIter {
         keep = __ballot_sync(0xFFFFFFFFu, take);
     }
     __device__ __forceinline__ void init() {
-        sb = s1 = s2 = s3 = sword = schunk = sbal = ssrc = sv = 0;
-        widx = wval = wn = wi = cur = curw = p = pend = 0;
+        sb = s0 = s1 = s2 = s3 = sc = sl = srem = 0;
+        widx = wval = wn = wi = wrem = p = pend = 0;
         boff = bcnt = bn = bi = keep = 0;
-        started = false;
+        started = done = false;
     }
     __device__ __forceinline__ uint32_t next() {
         while (p >= pend) {
