@@ -523,7 +523,9 @@ def run_workload(args):
     total_ms = max_over_ranks(sum(step_ms), world, "cuda")
     e2e = None
     if not args.no_e2e:
-        e2e = workloads.e2e(objs, dev, args.steps, max(1, args.warmup))
+        objs2 = workloads.upload(scs, dev)  # a second device copy to stream over
+        e2e = workloads.e2e(objs, dev, args.steps, max(1, args.warmup), objs2)
+        workloads.close(objs2)
         e2e_ms = max_over_ranks(1e3 * e2e.pop("seconds"), world, "cuda")
         e2e["value"] = replica_rate(frags_i * args.steps, world, e2e_ms)
         e2e["unit"] = "frags/s"
