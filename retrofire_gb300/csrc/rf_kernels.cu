@@ -221,14 +221,150 @@ __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t 
     }
 }
 
-// Sutherland-Hodgman for the queued triangles (clip.rs:283-301, 350-400),
-// one thread each; the polygon goes to a pool slot, its fan count to tcnt.
-__global__ void k_clip_poly(const DrawDev *__restrict__ draws,
-                            const float4 *__restrict__ cpos, const uint8_t *__restrict__ coc,
-                            uint32_t *__restrict__ tcnt, uint32_t *__restrict__ tpoly,
-                            const uint32_t *__restrict__ queue, PolyVert *__restrict__ pool,
-                            uint32_t pool_cap, uint32_t *__restrict__ counters) {
-    const uint32_t nq = counters[RF_CNT_CLIPQ];
+// Sutherland-Hodgman for the queued triangles (clip.rs:283-301, 350-400):
+// sixteen lanes per triangle, two triangles per warp, lane j holding polygon
+// vertex j.  Per plane each lane tests its vertex and its edge to vertex
+// j + 1 (the same operations as ClipPlane::clip_simple_polygon), a prefix
+// count over the group gives every output vertex its slot, and each lane
+// fetches its new vertex -- the kept vertex or the edge's intersection --
+// from the lane that produced it.  The output order is the reference's:
+// per edge in order, the kept start vertex, then the intersection.
+__device__ __forceinline__ void clip_groups(const DrawDev *__restrict__ draws, const float4 *__restrict__ cpos,
+                                            const uint8_t *__restrict__ coc, uint32_t *__restrict__ tcnt,
+                                            uint32_t *__restrict__ tpoly, const uint32_t *__restrict__ queue,
+                                            PolyVert *__restrict__ pool, uint32_t pool_cap,
+                                            uint32_t *__restrict__ counters, uint32_t nq) {
+    constexpr uint32_t FULL = 0xFFFFFFFFu;
+    static_assert(RF_POLY_CAP == 16, "one 16-lane group holds a polygon");
+    const uint32_t lane = threadIdx.x & 31u, j = lane & 15u, gb = lane & 16u;
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t qb = wid * 2u; qb < nq; qb += nw * 2u) {  // warp-uniform
+        const uint32_t qi = qb + (gb >> 4);
+        const bool have = qi < nq;
+        const uint32_t gt = have ? queue[qi] : 0u;
+        const uint32_t di = have ? tpoly[gt] : 0u;  // k_clip left the draw index there
+        const DrawDev &d = draws[di];
+        const uint32_t na = have ? (d.nattr < RF_MAX_ATTR ? d.nattr : RF_MAX_ATTR) : 0u;
+        float pos[4] = {0.0f, 0.0f, 0.0f, 1.0f}, a[RF_MAX_ATTR];
+#pragma unroll
+        for (int c = 0; c < RF_MAX_ATTR; ++c) a[c] = 0.0f;
+        uint32_t oc = 0;
+        if (have && j < 3u) {
+            const uint32_t vi = d.idx[3 * (size_t)(gt - d.tri_base) + j] + d.vert_base;
+            const float4 p = cpos[vi];
+            pos[0] = p.x; pos[1] = p.y; pos[2] = p.z; pos[3] = p.w;
+            const float *src = d.verts + (size_t)(vi - d.vert_base) * d.stride + d.pos_dim;
+#pragma unroll
+            for (int c = 0; c < RF_MAX_ATTR; ++c)
+                if ((uint32_t)c < na) a[c] = src[c];
+            oc = coc[vi];
+        }
+        uint32_t n = have ? 3u : 0u;
+        bool ovf = false;
+        for (int pl = 0; pl < 6; ++pl) {
+            const bool act = j < n;
+            const float dd = act ? dot4(c_planes[pl], pos) : 0.0f;
+            const bool in = act && (oc & (1u << pl)) == 0u;
+            // The edge to the next vertex (the first one closes the polygon).
+            const uint32_t nb = gb + (j + 1u < n ? j + 1u : 0u);
+            const float d1 = __shfl_sync(FULL, dd, nb);
+            float p1[4], a1[RF_MAX_ATTR];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) p1[c] = __shfl_sync(FULL, pos[c], nb);
+#pragma unroll
+            for (int c = 0; c < RF_MAX_ATTR; ++c) a1[c] = __shfl_sync(FULL, a[c], nb);
+            const bool cross = act && fmul(dd, d1) < 0.0f;  // ClipPlane::intersect (clip.rs:121-145)
+            float xp[4] = {0.0f, 0.0f, 0.0f, 0.0f}, xa[RF_MAX_ATTR];
+#pragma unroll
+            for (int c = 0; c < RF_MAX_ATTR; ++c) xa[c] = 0.0f;
+            uint32_t xoc = 0;
+            if (cross) {
+                const float t = fdiv(-dd, fsub(d1, dd));
+#pragma unroll
+                for (int c = 0; c < 4; ++c) xp[c] = lerp(pos[c], p1[c], t);
+#pragma unroll
+                for (int c = 0; c < RF_MAX_ATTR; ++c)
+                    if ((uint32_t)c < na) xa[c] = lerp(a[c], a1[c], t);
+                xoc = outcode(xp);
+            }
+            // Slots: an inclusive count over the group, then each output slot
+            // k = j finds the first lane whose count exceeds k.
+            const uint32_t cnt = (in ? 1u : 0u) + (cross ? 1u : 0u);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (uint32_t o = 1; o < 16u; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, incl, o, 16);
+                if (j >= o) incl += y;
+            }
+            const uint32_t total = __shfl_sync(FULL, incl, gb + 15u);
+            uint32_t sl = 0;
+#pragma unroll
+            for (uint32_t step = 8; step >= 1; step >>= 1) {
+                const uint32_t v = __shfl_sync(FULL, incl, gb + sl + step - 1u);
+                if (v <= j) sl += step;
+            }
+            const uint32_t src = gb + sl;
+            const uint32_t ex = __shfl_sync(FULL, incl - cnt, src);
+            const bool keep0 = __shfl_sync(FULL, in ? 1u : 0u, src) != 0u && j == ex;
+            float np_[4], na_[RF_MAX_ATTR];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float kv = __shfl_sync(FULL, pos[c], src), xv = __shfl_sync(FULL, xp[c], src);
+                np_[c] = keep0 ? kv : xv;
+            }
+#pragma unroll
+            for (int c = 0; c < RF_MAX_ATTR; ++c) {
+                const float kv = __shfl_sync(FULL, a[c], src), xv = __shfl_sync(FULL, xa[c], src);
+                na_[c] = keep0 ? kv : xv;
+            }
+            const uint32_t ko = __shfl_sync(FULL, oc, src), xo = __shfl_sync(FULL, xoc, src);
+            oc = keep0 ? ko : xo;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) pos[c] = np_[c];
+#pragma unroll
+            for (int c = 0; c < RF_MAX_ATTR; ++c) a[c] = na_[c];
+            if (total > RF_POLY_CAP) ovf = true;  // more vertices than the working buffer keeps
+            n = total < RF_POLY_CAP ? total : RF_POLY_CAP;
+        }
+        if (n > RF_POLY_STORE) ovf = true;
+        if (ovf) n = 0;  // only float pathologies get here; counted in stats.oob, dropped
+        uint32_t cntf = n >= 3u ? n - 2u : 0u, slot = RF_NO_POLY;
+        if (j == 0u && have) {
+            if (ovf) atomicAdd(&counters[RF_CNT_POLYOVF], 1u);
+            if (cntf) {
+                slot = atomicAdd(&counters[RF_CNT_POOL], 1u);
+                if (slot >= pool_cap) {
+                    atomicAdd(&counters[RF_CNT_POOLOVF], 1u);
+                    slot = RF_NO_POLY;
+                }
+            }
+        }
+        slot = __shfl_sync(FULL, slot, gb);
+        if (slot == RF_NO_POLY) cntf = 0;
+        if (have && slot != RF_NO_POLY && j < n) {
+            PolyVert *dst = pool + (size_t)slot * RF_POLY_STORE + j;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) dst->pos[c] = pos[c];
+#pragma unroll
+            for (int c = 0; c < RF_MAX_ATTR; ++c)
+                if ((uint32_t)c < na) dst->a[c] = a[c];
+        }
+        if (have && j == 0u) {
+            tcnt[gt] = cntf;
+            tpoly[gt] = slot;
+        }
+    }
+}
+
+// The same, one thread per triangle: for long queues, where whole warps of
+// triangles keep the SMs busy and the per-lane work of the groups would
+// cost more issue slots than it saves latency.
+__device__ __forceinline__ void clip_threads(const DrawDev *__restrict__ draws, const float4 *__restrict__ cpos,
+                                             const uint8_t *__restrict__ coc, uint32_t *__restrict__ tcnt,
+                                             uint32_t *__restrict__ tpoly, const uint32_t *__restrict__ queue,
+                                             PolyVert *__restrict__ pool, uint32_t pool_cap,
+                                             uint32_t *__restrict__ counters, uint32_t nq) {
     for (uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
         const uint32_t gt = queue[qi];
         const DrawDev &d = draws[tpoly[gt]];  // k_clip left the draw index there
@@ -284,6 +420,17 @@ __global__ void k_clip_poly(const DrawDev *__restrict__ draws,
         tcnt[gt] = cnt;
         tpoly[gt] = slot;
     }
+}
+
+#define RF_CLIP_GROUP_MAX 32768u  // queues up to this long are clipped by lane groups
+__global__ void __launch_bounds__(256)
+k_clip_poly(const DrawDev *__restrict__ draws, const float4 *__restrict__ cpos,
+            const uint8_t *__restrict__ coc, uint32_t *__restrict__ tcnt,
+            uint32_t *__restrict__ tpoly, const uint32_t *__restrict__ queue,
+            PolyVert *__restrict__ pool, uint32_t pool_cap, uint32_t *__restrict__ counters) {
+    const uint32_t nq = counters[RF_CNT_CLIPQ];
+    if (nq <= RF_CLIP_GROUP_MAX) clip_groups(draws, cpos, coc, tcnt, tpoly, queue, pool, pool_cap, counters, nq);
+    else clip_threads(draws, cpos, coc, tcnt, tpoly, queue, pool, pool_cap, counters, nq);
 }
 
 // ---------------------------------------------------------------------------
@@ -1171,8 +1318,8 @@ cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const fl
     k_clip<<<blocks, 256, 0, s>>>(draws, nd, nt, coc, tcnt, tpoly, queue, counters);
     // The queue's length is known on the device only: a grid for all of it
     // at the worst case, each thread striding over what is there.
-    const uint32_t pblocks = min((nt + 127) / 128, (uint32_t)nsm * 4);
-    k_clip_poly<<<pblocks, 128, 0, s>>>(draws, cpos, coc, tcnt, tpoly, queue, pool, pool_cap, counters);
+    const uint32_t pblocks = min((nt + 15) / 16, (uint32_t)nsm * 8);  // 16 triangles per block
+    k_clip_poly<<<pblocks, 256, 0, s>>>(draws, cpos, coc, tcnt, tpoly, queue, pool, pool_cap, counters);
     return cudaGetLastError();
 }
 
