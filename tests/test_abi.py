@@ -41,6 +41,14 @@ def test_python_bindings_cover_header(libpath):
     assert set(declared_symbols()) <= bound, set(declared_symbols()) - bound
 
 
+def test_rust_binding_covers_header():
+    """The -sys binding in INTEGRATION.md declares every entry point."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    bound = set(re.findall(r"\bfn (rf_[a-z_0-9]+)\s*\(", doc))
+    missing = [s for s in declared_symbols() if s not in bound]
+    assert not missing, missing
+
+
 def test_status_strings(libpath):
     L = rf.lib()
     assert L.rf_status_str(0) == b"ok"
