@@ -397,7 +397,8 @@ def run_gpu(args):
 # ------------------------------------------------- further workloads ---
 #
 # --workload picks one of the reference's other configurations; each prints
-# one JSON line with the same keys as the default.  Not the default line.
+# one JSON line with the same keys as the default; the headline line is the
+# default workload's.
 
 def _oracle_scene(sc):
     """Renders one bench scene dict with the oracle; returns Stats."""
