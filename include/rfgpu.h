@@ -126,6 +126,10 @@ rf_status rf_ctx_sync(rf_ctx *ctx);
 /* Adds the stats of every render since the last call into *out (and syncs). */
 rf_status rf_ctx_take_stats(rf_ctx *ctx, rf_stats *out);
 const char *rf_status_str(rf_status s);
+/* The CUDA call and error message behind the context's last RF_ERR_CUDA or
+ * RF_ERR_OOM ("" if none; "" for a NULL context).  Valid until the next call
+ * on the context. */
+const char *rf_ctx_last_error(const rf_ctx *ctx);
 /* Tile raster tuning: tile width in pixels (8, 16, 32 or 64; tiles are 32
  * rows high) and rasteriser warps per block.  0 keeps the current value. */
 rf_status rf_ctx_set_tiling(rf_ctx *ctx, uint32_t tile_w, uint32_t warps_per_block);

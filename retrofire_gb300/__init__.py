@@ -173,6 +173,8 @@ def lib():
             fn.restype = C.c_int32
         L.rf_status_str.argtypes = [C.c_int32]
         L.rf_status_str.restype = C.c_char_p
+        L.rf_ctx_last_error.argtypes = [_P]
+        L.rf_ctx_last_error.restype = C.c_char_p
         L.rf_obj_free.argtypes = [_P]
         L.rf_obj_free.restype = None
         _lib = L
@@ -259,6 +261,11 @@ class Device:
 
     def sync(self):
         _check(lib().rf_ctx_sync(self.ptr), "rf_ctx_sync")
+
+    def last_error(self):
+        """The CUDA call and message behind the last "cuda error" or "out of
+        device memory" status of this device ("" if none)."""
+        return lib().rf_ctx_last_error(self.ptr).decode()
 
     def set_tiling(self, tile_w=0, warps=0):
         _check(lib().rf_ctx_set_tiling(self.ptr, tile_w, warps), "rf_ctx_set_tiling")

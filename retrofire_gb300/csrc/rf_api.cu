@@ -755,6 +755,41 @@ rf_status flush_clear(rf_ctx *ctx, Target &tg) {
     return RF_OK;
 }
 
+// rf_mesh_upload (per = 3 indices per triangle) and rf_lines_upload (per =
+// 2 per line).  A failed allocation or copy frees what was allocated.
+rf_status upload_mesh(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
+                      uint32_t nattr, const uint32_t *idx, uint32_t nprim, uint32_t per,
+                      rf_mesh *out) {
+    if (!ctx || !out || (pos_dim != 3 && pos_dim != 4) || nattr > RF_MAX_ATTR) return RF_ERR_BAD_ARG;
+    if ((nverts && !verts) || (nprim && !idx)) return RF_ERR_BAD_ARG;
+    // `vs[i]` would panic on an index past the vertices (prim.rs:17-19, 53-55)
+    for (uint64_t i = 0; i < (uint64_t)per * nprim; ++i)
+        if (idx[i] >= nverts) return RF_ERR_BAD_ARG;
+    Mesh m;
+    m.nverts = nverts;
+    m.ntri = nprim;
+    m.pos_dim = pos_dim;
+    m.nattr = nattr;
+    m.lines = per == 2;
+    const size_t vb = (size_t)nverts * (pos_dim + nattr) * 4, ib = (size_t)nprim * per * 4;
+    cudaError_t e = cudaSuccess;
+    if (vb) e = cudaMalloc(&m.verts, vb);
+    if (e == cudaSuccess && ib) e = cudaMalloc(&m.idx, ib);
+    if (e == cudaSuccess && vb) e = cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && ib) e = cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(m.verts);
+        cudaFree(m.idx);
+        return cuda_fail(ctx, e, per == 2 ? "rf_lines_upload" : "rf_mesh_upload");
+    }
+    mesh_bbox(m, verts);
+    const uint64_t h = ctx->next_handle++;
+    ctx->meshes[h] = m;
+    *out = h;
+    return RF_OK;
+}
+
 rf_status finish_call(rf_ctx *ctx, rf_stats *out) {
     if (!out) return RF_OK;
     rf_stats tot{};
@@ -786,6 +821,10 @@ const char *rf_status_str(rf_status s) {
     }
 }
 
+const char *rf_ctx_last_error(const rf_ctx *ctx) {
+    return ctx ? ctx->last_error : "";
+}
+
 rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out) {
     if (!out) return RF_ERR_BAD_ARG;
     *out = nullptr;
@@ -797,9 +836,12 @@ rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out) {
     rf_ctx *ctx = new (std::nothrow) rf_ctx();
     if (!ctx) return RF_ERR_OOM;
     int dev = 0;
-    cudaGetDevice(&dev);
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        delete ctx;
+        return RF_ERR_CUDA;
+    }
     ctx->device = dev;
-    cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, dev);
     if (cuda_stream) {
         ctx->stream = (cudaStream_t)cuda_stream;
     } else {
@@ -917,51 +959,12 @@ rf_status rf_ctx_last_tiling(rf_ctx *ctx, uint32_t *tile_w, uint32_t *warps) {
 
 rf_status rf_mesh_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
                          uint32_t nattr, const uint32_t *idx, uint32_t ntri, rf_mesh *out) {
-    if (!ctx || !out || (pos_dim != 3 && pos_dim != 4) || nattr > RF_MAX_ATTR) return RF_ERR_BAD_ARG;
-    if ((nverts && !verts) || (ntri && !idx)) return RF_ERR_BAD_ARG;
-    for (uint64_t i = 0; i < 3ull * ntri; ++i)
-        if (idx[i] >= nverts) return RF_ERR_BAD_ARG;  // `vs[i]` would panic (prim.rs:17-19)
-    Mesh m;
-    m.nverts = nverts;
-    m.ntri = ntri;
-    m.pos_dim = pos_dim;
-    m.nattr = nattr;
-    const size_t vb = (size_t)nverts * (pos_dim + nattr) * 4, ib = (size_t)ntri * 12;
-    if (vb) CK(cudaMalloc(&m.verts, vb));
-    if (ib) CK(cudaMalloc(&m.idx, ib));
-    if (vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
-    if (ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    mesh_bbox(m, verts);
-    const uint64_t h = ctx->next_handle++;
-    ctx->meshes[h] = m;
-    *out = h;
-    return RF_OK;
+    return upload_mesh(ctx, verts, nverts, pos_dim, nattr, idx, ntri, 3, out);
 }
 
 rf_status rf_lines_upload(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t pos_dim,
                           uint32_t nattr, const uint32_t *idx, uint32_t nlines, rf_mesh *out) {
-    if (!ctx || !out || (pos_dim != 3 && pos_dim != 4) || nattr > RF_MAX_ATTR) return RF_ERR_BAD_ARG;
-    if ((nverts && !verts) || (nlines && !idx)) return RF_ERR_BAD_ARG;
-    for (uint64_t i = 0; i < 2ull * nlines; ++i)
-        if (idx[i] >= nverts) return RF_ERR_BAD_ARG;  // `vs[i]` would panic (prim.rs:53-55)
-    Mesh m;
-    m.nverts = nverts;
-    m.ntri = nlines;
-    m.pos_dim = pos_dim;
-    m.nattr = nattr;
-    m.lines = true;
-    const size_t vb = (size_t)nverts * (pos_dim + nattr) * 4, ib = (size_t)nlines * 8;
-    if (vb) CK(cudaMalloc(&m.verts, vb));
-    if (ib) CK(cudaMalloc(&m.idx, ib));
-    if (vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
-    if (ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    mesh_bbox(m, verts);
-    const uint64_t h = ctx->next_handle++;
-    ctx->meshes[h] = m;
-    *out = h;
-    return RF_OK;
+    return upload_mesh(ctx, verts, nverts, pos_dim, nattr, idx, nlines, 2, out);
 }
 
 rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_uniforms *u,
@@ -1122,9 +1125,13 @@ rf_status rf_texture_upload(rf_ctx *ctx, const uint32_t *rgba, uint32_t w, uint3
     t.w = w;
     t.h = h;
     const size_t b = (size_t)w * h * 4;
-    CK(cudaMalloc(&t.texels, b));
-    CK(cudaMemcpyAsync(t.texels, rgba, b, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    cudaError_t e = cudaMalloc(&t.texels, b);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t.texels, rgba, b, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(t.texels);
+        return cuda_fail(ctx, e, "rf_texture_upload");
+    }
     const uint64_t hd = ctx->next_handle++;
     ctx->textures[hd] = t;
     *out = hd;
@@ -1150,11 +1157,15 @@ rf_status rf_target_create(rf_ctx *ctx, uint32_t w, uint32_t h, int32_t pixfmt, 
     t.h = h;
     t.fmt = pixfmt;
     const size_t n = (size_t)w * h;
-    CK(cudaMalloc(&t.color, n * 4));
-    CK(cudaMemsetAsync(t.color, 0, n * 4, ctx->stream));
-    if (has_depth) {
-        CK(cudaMalloc(&t.depth, n * 4));
-        CK(cudaMemsetAsync(t.depth, 0, n * 4, ctx->stream));
+    cudaError_t e = cudaMalloc(&t.color, n * 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t.color, 0, n * 4, ctx->stream);
+    if (e == cudaSuccess && has_depth) e = cudaMalloc(&t.depth, n * 4);
+    if (e == cudaSuccess && has_depth) e = cudaMemsetAsync(t.depth, 0, n * 4, ctx->stream);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(t.color);
+        cudaFree(t.depth);
+        return cuda_fail(ctx, e, "rf_target_create");
     }
     const uint64_t hd = ctx->next_handle++;
     ctx->targets[hd] = t;

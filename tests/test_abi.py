@@ -37,7 +37,7 @@ def test_library_exports_all_declared(libpath):
 
 
 def test_python_bindings_cover_header(libpath):
-    bound = set(rf._SIGS) | {"rf_status_str", "rf_obj_free"}
+    bound = set(rf._SIGS) | {"rf_status_str", "rf_ctx_last_error", "rf_obj_free"}
     assert set(declared_symbols()) <= bound, set(declared_symbols()) - bound
 
 
@@ -53,6 +53,7 @@ def test_status_strings(libpath):
     L = rf.lib()
     assert L.rf_status_str(0) == b"ok"
     assert L.rf_status_str(3).startswith(b"texture")
+    assert L.rf_ctx_last_error(None) == b""
 
 
 def test_no_device_reports_status(libpath):
