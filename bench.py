@@ -579,7 +579,8 @@ def run_serve(args):
         res, wall = serve.run_load(srv, ms, reqs, realtime=True, depth=False)
         clk = clocks.stop()
         s = serve.latency_summary(res)
-        lines.append((rate, len(reqs), wall, s, srv.counts(), clk))
+        d2h = sum(4 * r["w"] * r["h"] for r in reqs) // len(reqs)  # colour read back per request
+        lines.append((rate, len(reqs), wall, s, srv.counts(), clk, d2h))
         srv.close()
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -587,8 +588,8 @@ def run_serve(args):
         cpu = {"value": it, "unit": "requests/s", "cores": 1, "kind": "port",
                "sample": "60 requests of the stream rendered by the oracle, single thread, %.1f s" % t}
     if rank == 0:
-        rate, n, wall, s, c, clk = lines[-1]
-        h2d = 0
+        rate, n, wall, s, c, clk, d2h = lines[-1]
+        h2d = 0  # meshes are preloaded handles; a request uploads only its draw records
         line = {"metric": "requests/s", "value": n / wall, "unit": "requests/s", "n_gpus": world,
                 "steps": n, "warmup": 40, "ms_per_step": 1e3 * wall / n, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -600,9 +601,9 @@ def run_serve(args):
                            "readback": "colour to host per request"},
                 "latency_ms": {"p50": s["p50_ms"], "p99": s["p99_ms"]},
                 "per_rate": [{"rate": r, "served_per_s": nn / w, **ss, **cc}
-                             for r, nn, w, ss, cc, _ in lines],
+                             for r, nn, w, ss, cc, _, _ in lines],
                 "e2e": {"value": n / wall, "unit": "requests/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": None},
+                        "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu, "roofline": None, "gpu_launches": None, "clocks": clk}
         print(json.dumps(line))
     ms.close()
