@@ -153,6 +153,10 @@ namespace {
 
 rf_status cuda_fail(rf_ctx *c, cudaError_t e, const char *what) {
     if (c) snprintf(c->last_error, sizeof c->last_error, "%s: %s", what, cudaGetErrorString(e));
+    // A failed call (an allocation, say) leaves the runtime's last-error
+    // state set; the launches of a later call check that state, so clear it
+    // here (a sticky error keeps failing every later call anyway).
+    cudaGetLastError();
     return e == cudaErrorMemoryAllocation ? RF_ERR_OOM : RF_ERR_CUDA;
 }
 

@@ -99,9 +99,14 @@ uint32_t pack(uint32_t c, int32_t fmt) {
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_rf_noalloc_scratch[RF_NOALLOC_SCRATCH_BYTES];
 
+// On failure the runtime's last-error state is cleared too, so the
+// launches of a later call do not report this error as theirs.
 #define NA_CK(call)                              \
     do {                                         \
-        if ((call) != cudaSuccess) return RF_ERR_CUDA; \
+        if ((call) != cudaSuccess) {             \
+            cudaGetLastError();                  \
+            return RF_ERR_CUDA;                  \
+        }                                        \
     } while (0)
 
 extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint32_t pos_dim,
@@ -142,8 +147,10 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
         std::lock_guard<std::mutex> lk(g_mu);
         if (!g_addr[dev]) {
             void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_rf_noalloc_scratch) != cudaSuccess || !p)
+            if (cudaGetSymbolAddress(&p, g_rf_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
                 return RF_ERR_CUDA;
+            }
             g_addr[dev] = p;
         }
         base = static_cast<unsigned char *>(g_addr[dev]);

@@ -157,10 +157,12 @@ void serve(rf_server *S, std::vector<Req> &batch, uint64_t batch_id) {
         S->stage = nullptr;
         S->stage_cap = 0;
         const size_t cap = need + need / 2;
-        if (cudaHostAlloc(reinterpret_cast<void **>(&S->stage), cap, cudaHostAllocDefault) == cudaSuccess)
+        if (cudaHostAlloc(reinterpret_cast<void **>(&S->stage), cap, cudaHostAllocDefault) == cudaSuccess) {
             S->stage_cap = cap;
-        else
+        } else {
             S->stage = nullptr;
+            cudaGetLastError();  // the direct reads below stand in; later launches must not see it
+        }
     }
     if (S->stage && need <= S->stage_cap) {
         staged = true;
