@@ -138,7 +138,7 @@ struct rf_ctx {
     // already handed out by rf_ctx_take_stats / rf_render
     rf_stats host_acc{};
     rf_stats taken{};
-    char last_error[256] = {0};
+    char last_error[1024] = {0};  // the failing call (as written) and the CUDA message
     std::vector<DrawDev> hdraws;
     std::vector<JobDev> hjobs;
     // stage timing
