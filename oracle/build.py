@@ -1,6 +1,6 @@
 """Build recipe for the C++ oracle shared library (test infrastructure).
 
-g++ -O2 -ffp-contract=off: Rust never fuses a*b+c, and aarch64 GCC would
+g++ -O3 -ffp-contract=off: Rust never fuses a*b+c, and aarch64 GCC would
 otherwise contract to FMA by default, silently breaking bit-exact parity.
 """
 import os
@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "librforacle.so")
 SRCS = [os.path.join(HERE, "rf_oracle.cpp")]
-FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
+FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
          "-fPIC", "-shared", "-Wall", "-Wextra"]
 
 

@@ -721,7 +721,7 @@ namespace {
 template <int NA>
 uint32_t tri_fill_test(const float *screen, const float *attr, uint32_t zmask, uint64_t *rows,
                        uint32_t max_rows, float *frags, uint64_t max_frags, uint64_t *nfrags) {
-    Var<NA> v[3];
+    Var<NA> v[3]{};
     for (int k = 0; k < 3; ++k) {
         for (int c = 0; c < 3; ++c) v[k].p[c] = screen[3 * k + c];
         for (int a = 0; a < NA; ++a) v[k].a[a] = attr[NA * k + a];
