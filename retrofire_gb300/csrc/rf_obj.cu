@@ -4,7 +4,9 @@
 // :309-370): the same items, the same quad split, the same vertex
 // de-duplication by (position, texcoord, normal) index triple in order of
 // first use, the same errors (as status codes, where the reader panics too).
-#include <cerrno>
+#include <locale.h>
+#include <stdlib.h>
+
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -43,14 +45,51 @@ std::vector<std::string> tokens_of(const char *b, const char *e) {
     return out;
 }
 
-// f32 parsing: a complete decimal or special token, correctly rounded.
+// The grammar of Rust's f32::from_str: Sign? ('inf' | 'infinity' | 'nan' |
+// Number), the words in any case; Number = (Digit+ | Digit+ '.' Digit* |
+// Digit* '.' Digit+) Exp?; Exp = ('e' | 'E') Sign? Digit+.  (No hexadecimal
+// forms, no "nan(...)" payloads, no spaces.)
+bool is_digit(char c) { return c >= '0' && c <= '9'; }
+bool rust_f32_syntax(const std::string &t) {
+    size_t i = 0;
+    const size_t n = t.size();
+    if (i < n && (t[i] == '+' || t[i] == '-')) ++i;
+    std::string word;
+    for (size_t k = i; k < n; ++k) word += (char)((t[k] >= 'A' && t[k] <= 'Z') ? t[k] - 'A' + 'a' : t[k]);
+    if (word == "inf" || word == "infinity" || word == "nan") return true;
+    size_t digits = 0;
+    while (i < n && is_digit(t[i])) ++i, ++digits;
+    if (i < n && t[i] == '.') {
+        ++i;
+        while (i < n && is_digit(t[i])) ++i, ++digits;
+    }
+    if (digits == 0) return false;
+    if (i < n && (t[i] == 'e' || t[i] == 'E')) {
+        ++i;
+        if (i < n && (t[i] == '+' || t[i] == '-')) ++i;
+        size_t ed = 0;
+        while (i < n && is_digit(t[i])) ++i, ++ed;
+        if (ed == 0) return false;
+    }
+    return i == n;
+}
+
+// The "C" locale, so that the decimal point is '.' whatever locale the
+// calling process has set.
+locale_t c_locale() {
+    static const locale_t loc = newlocale(LC_NUMERIC_MASK, "C", (locale_t)0);
+    return loc;
+}
+
+// f32 parsing as Rust's f32::from_str: its grammar, then the correctly
+// rounded value (strtof; out of range gives +-inf or +-0 as Rust does).
 float parse_f32(const std::string &t) {
-    if (t.empty()) throw ObjErr{"invalid numeric value"};
+    if (!rust_f32_syntax(t)) throw ObjErr{"invalid numeric value"};
     char *end = nullptr;
-    errno = 0;
-    const float v = strtof(t.c_str(), &end);
+    const locale_t loc = c_locale();
+    const float v = loc ? strtof_l(t.c_str(), &end, loc) : strtof(t.c_str(), &end);
     if (end != t.c_str() + t.size()) throw ObjErr{"invalid numeric value"};
-    return v;  // overflow gives +-inf like Rust's parse
+    return v;
 }
 
 // usize parsing ("+" allowed, digits only), then OBJ's one-based index.

@@ -55,6 +55,25 @@ def test_float_formats():
     assert v[2, 0] == np.float32(0.015)
 
 
+def test_float_words_and_range():
+    """Rust's f32::from_str: inf / infinity / nan in any case, with a sign;
+    out-of-range decimals round to +-inf or +-0."""
+    v, _ = rf.parse_obj("v inf -Infinity NaN\nv 1e50 -1e-50 +.5\nv 3.4028235e38 1e-45 7\nf 1 2 3\n")
+    assert np.isposinf(v[0, 0]) and np.isneginf(v[0, 1]) and np.isnan(v[0, 2])
+    assert np.isposinf(v[1, 0]) and v[1, 1] == 0.0 and np.signbit(v[1, 1]) and v[1, 2] == 0.5
+    assert v[2, 0] == np.finfo(np.float32).max and v[2, 1] == np.float32(1e-45)
+
+
+@pytest.mark.parametrize("tok", ["0x1p3", "0X10", ".", "e5", "1e", "1.5e+", "--1", "1..2", "1e5.5",
+                                 "nan(1)", "infinit", "1_000", "1f", ",5"])
+def test_float_syntax_rejected(tok):
+    """Forms Rust's f32 parser rejects (hexadecimal, C's nan payloads, a
+    missing mantissa or exponent) are invalid numeric values here too."""
+    with pytest.raises(rf.ObjError) as e:
+        rf.parse_obj("v %s 0 0\n" % tok)
+    assert "invalid numeric" in str(e.value)
+
+
 @pytest.mark.parametrize("src", ["", "   \n\t\n", "# only\n# comments\n"])
 def test_empty_inputs(src):
     v, f = rf.parse_obj(src)
