@@ -1,5 +1,8 @@
 """Host side of the serving workload (no GPU): the request stream's
-arrival process and mix, the camera and mesh builders."""
+arrival process and mix, the camera and mesh builders, and the load driver
+(arrival pacing, result order, error propagation) over a stand-in server."""
+import time
+
 import numpy as np
 
 import retrofire_gb300 as rf
@@ -62,3 +65,56 @@ def test_orbit_camera_keeps_grid_visible():
         st = O.render([d], mat.viewport(0, 240, 320, 0), col, dep, {})
         hit += st.prims_o >= 100
     assert hit >= 8
+
+
+class _FakeServer:
+    """Stands in for rf.Server on the host: tickets in submission order,
+    results carrying the submit time, an error planted at one request."""
+
+    def __init__(self, fail_at=None):
+        self.sub, self.fail_at, self.n = {}, fail_at, 0
+
+    def submit(self, draws, vp, w, h, ctx=None, pixfmt=0, depth=True):
+        if self.n == self.fail_at:
+            raise rf.RfError(2, "rf_server_submit")
+        self.n += 1
+        self.sub[self.n] = (time.perf_counter(), w, h, draws)
+        return self.n
+
+    def wait(self, ticket):
+        t, w, h, draws = self.sub.pop(ticket)
+        res = {"total_ms": 1.0 + ticket, "queue_ms": 0.5, "batch_size": 1 + ticket % 3,
+               "submitted": t, "draws": draws}
+        return np.zeros((h, w), np.uint32), None, res
+
+
+class _FakeMeshSet:
+    def draws(self, req):
+        return [("mesh%d" % req["mesh"], None, req["mvp"])]
+
+
+def test_run_load_paces_arrivals_and_keeps_order():
+    from retrofire_gb300 import serve
+    reqs = scenes.serving_requests(40, 400.0, seed=11)
+    srv = _FakeServer()
+    t0 = time.perf_counter()
+    out, wall = serve.run_load(srv, _FakeMeshSet(), reqs, realtime=True)
+    assert len(out) == len(reqs) and wall >= reqs[-1]["t"] * 0.95
+    for i, (r, (c, d, res)) in enumerate(zip(reqs, out)):
+        assert c.shape == (r["h"], r["w"]) and res["draws"][0][0] == "mesh%d" % r["mesh"]
+        # submitted no earlier than its arrival offset
+        assert res["submitted"] - t0 >= r["t"] - 1e-3
+    s = serve.latency_summary(out)
+    assert s["p50_ms"] == np.percentile([2.0 + i for i in range(40)], 50)
+    assert s["max_batch"] == 3 and s["queue_p99_ms"] == 0.5
+
+
+def test_run_load_surfaces_a_submit_error():
+    from retrofire_gb300 import serve
+    reqs = scenes.serving_requests(10, 1000.0, seed=12)
+    try:
+        serve.run_load(_FakeServer(fail_at=4), _FakeMeshSet(), reqs, realtime=False)
+    except rf.RfError as e:
+        assert e.code == 2
+    else:
+        raise AssertionError("the producer's error was not raised")
