@@ -1,6 +1,7 @@
 """bench.py's output contract on the CPU: the reference arm prints one JSON
-line with the keys of the default line, and the GPU arm fails loudly
-without a GPU (no CPU fallback)."""
+line with the keys of the default line, the GPU arm fails loudly without a
+GPU (no CPU fallback), and the clock samples taken during the timed region
+are summarised as the clocks key."""
 import json
 import os
 import subprocess
@@ -44,3 +45,30 @@ def test_gpu_arm_fails_loudly_without_a_gpu():
     p = _bench("--steps", "1", "--warmup", "1")
     assert p.returncode != 0
     assert not [l for l in p.stdout.splitlines() if l.startswith("{")]
+
+
+def test_clock_samples_parsed():
+    """The clocks key: median SM clock, the maximum, and the throttle reasons
+    seen active, from nvidia-smi's CSV samples (here a stand-in process)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    csv = "\n".join([
+        "0, 2070, 2070, 812.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1965, 2070, 1398.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2055, 2070, 1200.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, [N/A], 2070, 0.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+    ])
+
+    class Proc:
+        def terminate(self):
+            pass
+
+        def communicate(self, timeout=None):
+            return csv, None
+
+    c = bench.Clocks(0)
+    c.p = Proc()
+    r = c.stop()
+    assert r == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert bench.Clocks(0).stop() is None  # never started
