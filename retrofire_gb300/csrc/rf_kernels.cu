@@ -832,14 +832,14 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
             __syncwarp();
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
             const uint32_t dst = p0 + c;
-            if (bal) {  // append this round's live triangles to the list
+            if (bal) {  // append this step's live triangles to the list
                 const uint32_t lead = __ffs(bal) - 1;
                 uint32_t at = 0;
                 if (lane == lead) at = atomicAdd(live_n, (uint32_t)__popc(bal));
                 at = __shfl_sync(0xFFFFFFFFu, at, lead);
                 if (keep) live[at + __popc(bal & ((1u << lane) - 1u))] = dst;
             }
-            // Write out the records built in this round, one per pass.
+            // Write out the records built in this step, one per pass.
             while (bal) {
                 const uint32_t l = __ffs(bal) - 1;
                 bal &= bal - 1;
