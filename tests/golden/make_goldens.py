@@ -18,6 +18,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_REF = "/root/reference"
 
 
 def parse_ppm(data):
@@ -44,12 +45,12 @@ def raw_string_after(src, fn_name):
     return m.group(1)
 
 
-def main(ref):
+def main(ref, out_dir=HERE):
     out = {}
     for name, rel in [("textured_quad", "core/tests/textured_quad.ppm"),
                       ("triangle", "core/triangle.ppm")]:
         img = parse_ppm(open(os.path.join(ref, rel), "rb").read())
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), rgb=img)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), rgb=img)
     raster = open(os.path.join(ref, "core/src/render/raster.rs")).read()
     out["shared_edge"] = raw_string_after(raster, "shared_edge_should_not_have_gaps_or_overdraw")
     out["gradient"] = raw_string_after(raster, "gradient")
@@ -57,9 +58,9 @@ def main(ref):
     m = re.search(r"out_tris,\s*\[([0-9,\s]+)\]", clip)
     out["clip_histogram"] = [int(x) for x in m.group(1).split(",") if x.strip()]
     out["source"] = "retrofire reference tree; see make_goldens.py docstring"
-    with open(os.path.join(HERE, "reference_vectors.json"), "w") as f:
+    with open(os.path.join(out_dir, "reference_vectors.json"), "w") as f:
         json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF)
