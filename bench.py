@@ -18,6 +18,15 @@ e2e     the same metric through the C ABI with host buffers: per step the
 roofline  achieved = algorithmic bytes of the tile rasteriser per frame
         (4 frags.i + 8 frags.o + 8 W H) / its CUDA-event time; peak = the
         measured HBM copy bandwidth.
+batch   the metric's own comparison on the 256 uneven scenes: one
+        rf_render_batch per step (CUDA graphs on) against the plain per-frame
+        drop-in, one rf_render_draws per scene, on the same targets, timed the
+        same way (CUDA events, L2 flush between steps); both legs' images and
+        stats are compared bit for bit before timing.
+serve   a Poisson request stream at a fixed rate through rf_server (continuous
+        batching) against the plain per-frame loop (one request at a time:
+        clear, rf_render_draws, read back): frames/s and p50/p99 latency from
+        arrival to the image in host memory.
 
 --impl reference times the reference's CPU path (the C++ oracle, a
 restatement of retrofire's render(); Rust is not available here) on the
@@ -29,6 +38,8 @@ import os
 import subprocess
 import sys
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -286,6 +297,121 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
                            "note": "one synchronous step: upload, render, read back"}}
 
 
+def batch_leg(args, dev, stream, flush, local):
+    """C4 batched vs the plain per-frame drop-in (see the module doc)."""
+    import torch
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import workloads
+    scs = workloads.scenes_for("batch")
+    objs = workloads.upload(scs, dev)
+    batch = objs["scenes"]
+    targets = objs["targets"]
+
+    def clear_all():
+        for tg in targets:
+            tg.clear()
+
+    # Parity of the two legs (untimed): every scene's image and stats.
+    clear_all()
+    st_b = rf.render_batch(batch, device=dev)
+    dig_b = workloads.target_digests(targets)
+    clear_all()
+    st_f = workloads.render_per_frame(batch, dev, sync_stats=True)
+    dig_f = workloads.target_digests(targets)
+    bad_img = [i for i, (a, b) in enumerate(zip(dig_b, dig_f)) if a != b]
+    bad_st = [i for i, (a, b) in enumerate(zip(st_b, st_f)) if a.as_dict() != b.as_dict()]
+    same = not bad_img and not bad_st
+    mismatch = None if same else {
+        "images": bad_img[:16], "n_images": len(bad_img), "stats": bad_st[:16], "n_stats": len(bad_st),
+        "first_stats": [st_b[bad_st[0]].as_dict(), st_f[bad_st[0]].as_dict()] if bad_st else None}
+    frags_i = sum(x.frags_i for x in st_b)
+    frags_o = sum(x.frags_o for x in st_b)
+    px = sum(sc["w"] * sc["h"] for sc in scs)
+    ntri = sum(len(d["faces"]) for sc in scs for d in sc["draws"])
+
+    def timed(step, graphs):
+        dev.set_graphs(graphs)
+        for _ in range(TUNE_FRAMES):  # online tiling settles per frame shape (untimed)
+            step()
+        step_ms, _, launches, clk = device_time(dev, stream, step, args.steps, args.warmup, flush,
+                                                local, stages=False)
+        dev.set_graphs(False)
+        ms = sum(step_ms) / len(step_ms)
+        return {"ms_per_step": ms, "frags_per_s": frags_i / (ms / 1e3),
+                "tris_per_s": ntri / (ms / 1e3), "frames_per_s": len(scs) / (ms / 1e3),
+                "gpu_launches_per_step": launches / args.steps, "clocks": clk}
+
+    def batched():
+        clear_all()
+        rf.render_batch(batch, device=dev, sync_stats=False)
+
+    def per_frame():
+        clear_all()
+        workloads.render_per_frame(batch, dev)
+
+    b = timed(batched, True)
+    b.update(graphs=True, tile_w=dev.last_tiling()[0], calls_per_step=1)
+    f = timed(per_frame, False)
+    f.update(graphs=False, calls_per_step=len(scs))
+    peak, peak_kind = measured_peak()
+    alg = 4 * frags_i + 8 * frags_o + 8 * px
+    workloads.close(objs)
+    return {"workload": "uneven_batch_256", "scenes": len(scs), "triangles": ntri,
+            "frags_i_per_step": frags_i, "frags_o_per_step": frags_o,
+            "batched": b, "per_frame": f,
+            "batched_vs_per_frame": f["ms_per_step"] / b["ms_per_step"],
+            "batched_model_gbs": alg / (b["ms_per_step"] / 1e3) / 1e9,
+            "peak_gbs": peak, "peak_kind": peak_kind,
+            "parity_checked": {"batched_equals_per_frame": bool(same), "scenes": len(scs),
+                               "mismatch": mismatch,
+                               "what": "colour + depth images (blake2b) and per-scene stats, "
+                                       "bit for bit",
+                               "oracle": "every scene bit-exact against the oracle in "
+                                         "tests/test_gpu_fullsize.py"},
+            "l2": "flushed between steps (512 MiB write)" if flush is not None else "not flushed"}
+
+
+def serve_leg(args, dev):
+    """C5 served vs the plain per-frame request loop at one rate."""
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import scenes, serve
+    rate = args.serve_rate
+    n = max(50, int(rate * args.duration))
+    reqs = scenes.serving_requests(n, rate, seed=100 + int(rate))
+    ms = serve.MeshSet(dev)
+    warm = scenes.serving_requests(60, rate, seed=7)
+    out = {"rate_per_s": rate, "requests": n, "duration_s": args.duration,
+           "meshes": [m[0] for m in scenes.SERVING_MESHES],
+           "resolutions": scenes.SERVING_RESOLUTIONS,
+           "target": "ARGB8888 + f32 depth, depth test on (Context::default)",
+           "readback": "colour to host per request"}
+    srv = rf.Server(dev, hbm_budget_bytes=64 << 30, inflight=args.inflight)
+    try:
+        serve.run_load(srv, ms, warm, realtime=False, read_depth=False)
+        res, wall = serve.run_load(srv, ms, reqs, realtime=True, read_depth=False)
+        mem = srv.memory()
+    finally:
+        srv.close()
+    s = serve.latency_summary(res)
+    fr = sum(r[2]["stats"].frags_i for r in res)
+    out["served"] = dict(s, frames_per_s=n / wall, frags_per_s=fr / wall, inflight=args.inflight,
+                         peak_inflight=mem["peak_inflight"], peak_charged_gb=mem["peak_charged"] / 1e9)
+    serve.run_per_frame(dev, ms, warm, realtime=False)
+    res_f, wall_f = serve.run_per_frame(dev, ms, reqs, realtime=True)  # depth targets, colour read
+    sf = serve.latency_summary(res_f)
+    fr_f = sum(r[2]["stats"].frags_i for r in res_f)
+    out["per_frame"] = dict(sf, frames_per_s=n / wall_f, frags_per_s=fr_f / wall_f)
+    same = all(np.array_equal(a[0], b[0]) for a, b in zip(res, res_f)) and \
+        all(a[2]["stats"].as_dict() == b[2]["stats"].as_dict() for a, b in zip(res, res_f))
+    out["parity_checked"] = {"served_equals_per_frame": bool(same), "requests": n,
+                             "what": "colour images and stats of every request, bit for bit"}
+    out["served_vs_per_frame"] = {"frames_per_s": out["served"]["frames_per_s"] /
+                                  out["per_frame"]["frames_per_s"],
+                                  "p99_ms": out["per_frame"]["p99_ms"] / out["served"]["p99_ms"]}
+    ms.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     rank, world, local = dist_env()
@@ -360,6 +486,14 @@ def run_gpu(args):
     if not args.no_e2e:
         e2e = run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world)
 
+    bleg = sleg = None
+    if rank == 0 and not args.no_batch:
+        bleg = batch_leg(args, dev, stream, flush, local)
+    if rank == 0 and not args.no_serve:
+        sleg = serve_leg(args, rf.Device())
+    if world > 1:
+        torch.distributed.barrier()
+
     if rank == 0:
         peak, peak_kind = measured_peak()
         raster_ms = stage["raster"] / max(nfr, 1)
@@ -385,6 +519,8 @@ def run_gpu(args):
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
+            "batch": bleg,
+            "serve": sleg,
         }
         print(json.dumps(line))
     for o in (mesh, tg):
@@ -572,11 +708,11 @@ def run_serve(args):
     lines = []
     for rate in args.rates:
         reqs = scenes.serving_requests(int(rate * args.duration), float(rate), seed=100 + int(rate))
-        srv = rf.Server(dev, hbm_budget_bytes=64 << 30)
-        serve.run_load(srv, ms, reqs[:40], realtime=False, depth=False)  # warm-up
+        srv = rf.Server(dev, hbm_budget_bytes=64 << 30, inflight=args.inflight)
+        serve.run_load(srv, ms, reqs[:40], realtime=False, read_depth=False)  # warm-up
         clocks = Clocks(local)
         clocks.start()
-        res, wall = serve.run_load(srv, ms, reqs, realtime=True, depth=False)
+        res, wall = serve.run_load(srv, ms, reqs, realtime=True, read_depth=False)
         clk = clocks.stop()
         s = serve.latency_summary(res)
         d2h = sum(4 * r["w"] * r["h"] for r in reqs) // len(reqs)  # colour read back per request
@@ -659,7 +795,19 @@ def main():
                          "batch: 256 uneven scenes in one pass; serve: Poisson request stream")
     ap.add_argument("--rates", type=float, nargs="+", default=[200.0, 1000.0, 2000.0])
     ap.add_argument("--duration", type=float, default=2.0)
+    ap.add_argument("--serve-rate", type=float, default=1000.0,
+                    help="request rate of the default line's served-vs-per-frame leg")
+    ap.add_argument("--inflight", type=int, default=2, help="serving pipelines")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-per-frame leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-per-frame leg")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # --gpus N without a launcher: start N replicas (one process per GPU)
+        # the way the multi-GPU runs are launched, and report their line.
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+               "--nproc-per-node", str(args.gpus), "--master-addr", "127.0.0.1",
+               "--master-port", str(29500 + os.getpid() % 1000), os.path.abspath(__file__)] + sys.argv[1:]
+        sys.exit(subprocess.call(cmd))
     if args.impl == "reference":
         if args.workload == "fill":
             run_reference(args)

@@ -75,15 +75,23 @@ typedef struct {
     rf_texture texture;   /* RF_SHADER_TEXTURED / RF_SHADER_TEX_GOURAUD */
 } rf_uniforms;
 
+/* Context::depth_sort (ctx.rs:39, render.rs:180-182, 209-219): None,
+ * Some(FrontToBack), Some(BackToFront). */
+enum { RF_SORT_NONE = 0, RF_SORT_FRONT_TO_BACK = 1, RF_SORT_BACK_TO_FRONT = 2 };
+
 /* Context (ctx.rs:11-65) without the clears (rf_target_clear) and stats
- * (returned in rf_stats).  Context::default() == {LESS, 1, 1, BACK}.
- * depth_sort is not supported: the reference sorts with sort_unstable_by,
- * whose order of equal keys is unspecified. */
+ * (returned in rf_stats).  Context::default() == {LESS, 1, 1, BACK, NONE}.
+ * depth_sort orders each render() call's clipped triangles by their mean
+ * clip-space z (Render::depth, prim.rs:21-23) under f32::total_cmp before
+ * setup, as depth_sort() does.  The reference sorts with sort_unstable_by,
+ * whose order of equal keys is unspecified; here the sort is stable, so
+ * triangles of equal depth keep their submission (and fan) order. */
 typedef struct {
     int32_t depth_test;
     int32_t color_write;
     int32_t depth_write;
     int32_t face_cull;
+    int32_t depth_sort;
 } rf_context_flags;
 
 /* Stats / Throughput (render/stats.rs:16-40).  oob counts scanlines that
@@ -272,8 +280,9 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
 /* ---- rendering without device allocation ------------------------------
  * No counterpart in the reference: retrofire allocates freely on the CPU.
  * For callers that must not call cudaMalloc while rendering — a frame loop
- * held to a fixed, pre-reserved device-memory budget, a plugin inside a host
- * application that owns all allocations, code recording into a CUDA graph.
+ * held to a fixed, pre-reserved device-memory budget, or a plugin inside a
+ * host application that owns every allocation and only lends the plugin the
+ * buffers to read and fill.
  * One render() call like rf_render, but every buffer is the caller's device
  * memory (verts, idx, texture, colour, optional depth) and the temporaries
  * live in a fixed scratch area of RF_NOALLOC_SCRATCH_BYTES compiled into the
@@ -283,8 +292,11 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
  * larger inputs return RF_ERR_OVER_BUDGET.
  * The first call on a device looks up the scratch area's device address
  * (once per device, with that device current), so make that first call
- * before any stream capture.  All calls share the one area: calls whose GPU
- * work overlaps race and give wrong results — order them on one stream.
+ * before any stream capture; the address is kept until exit, so the call
+ * must not be used on a device after cudaDeviceReset.  All calls share the
+ * one area: calls whose GPU work overlaps race and give wrong results —
+ * order them on one stream.  ntri > 0 with nverts == 0, and a depth_sort
+ * other than RF_SORT_NONE, are RF_ERR_BAD_ARG.
  * clear_rgba / depth_clear (nullable) apply Frame::clear first.  stats,
  * when non-NULL, waits for the stream and receives this call's stats.
  * cuda_stream may be NULL (the legacy default stream). */
@@ -325,34 +337,50 @@ rf_status rf_mesh_load_obj(rf_ctx *ctx, const char *text, size_t len, int32_t at
 /* ---- serving loop -----------------------------------------------------
  * No counterpart in the reference, which renders one frame per call on
  * the caller's thread (render.rs:134).  A server takes over an rf_ctx
- * whose meshes and textures are already uploaded and runs a worker thread
- * on it.  Any thread submits requests: a scene (draws on the context's
- * meshes and textures, a viewport, context flags), a target size and
- * format, the Frame::clear values and host buffers for the image.
+ * whose meshes and textures are already uploaded.  Any thread submits
+ * requests: a scene (draws on the context's meshes and textures, a
+ * viewport, context flags), a target size and format, the Frame::clear
+ * values and host buffers for the image.
+ *
+ * Continuous batching: the server runs `inflight` pipelines (default 2),
+ * each a worker thread with its own CUDA stream, scratch arenas, pooled
+ * targets and pre-sized page-locked staging, all reading the context's
+ * meshes and textures.  Whenever a pipeline is free it takes, in arrival
+ * order, the queued requests that fit what is left of the device-memory
+ * budget (at most max_batch requests, max_batch_tris input triangles and
+ * its staging room; the first always goes) and queues them as one
+ * rf_render_batch, then their read-backs, on its stream; while it waits for
+ * the GPU, the other pipelines admit the requests that arrived meanwhile,
+ * so their work overlaps on the device.
  *
  * Admission: each request is charged an estimate of the device memory it
- * needs (its target plus RF_SERVE_BYTES_PER_TRI per input triangle and
- * RF_SERVE_BYTES_PER_VERT per vertex of scratch); a request whose estimate
- * alone exceeds the budget is refused at submit (RF_ERR_OVER_BUDGET).
- * Continuous batching: the worker takes, in arrival order, every queued
- * request that fits the budget (at most max_batch), renders them with one
- * rf_render_batch into pooled targets, copies each image into its host
- * buffers and completes the requests; requests that arrive meanwhile form
- * the next batch.  A request's image and stats equal rf_render_draws of
- * its scene alone on a cleared target, whatever batch it lands in.  A
- * request that fails validation (bad handle, bad argument) fails alone.
+ * holds while in flight: its target, RF_SERVE_BYTES_PER_TRI per input
+ * triangle and RF_SERVE_BYTES_PER_VERT per vertex of scratch, and its tile
+ * masks (one bit per input triangle per 8x32-pixel tile).  A batch is
+ * admitted while the charges of every batch in flight stay within the
+ * budget; a request whose charge alone exceeds it is refused at submit
+ * (RF_ERR_OVER_BUDGET).
+ *
+ * A request's image and stats equal rf_render_draws of its scene alone on a
+ * cleared target, whatever batch or pipeline it lands in.  A request that
+ * fails validation (bad handle, bad argument) fails alone.
  *
  * While a server runs, the context belongs to it: the caller makes no
  * other call on that context until rf_server_destroy, which drains the
- * queue, joins the worker and frees the pooled targets (the context and
- * its meshes and textures stay the caller's). */
+ * queue, joins the workers and frees the pipelines (the context and its
+ * meshes and textures stay the caller's). */
 #define RF_SERVE_BYTES_PER_TRI 5632u
 #define RF_SERVE_BYTES_PER_VERT 24u
 typedef struct rf_server rf_server;
 typedef struct {
     uint64_t hbm_budget_bytes; /* 0: 64 GiB */
-    uint32_t max_batch;        /* 0: 256 */
-    uint32_t reserved_;
+    uint32_t max_batch;        /* requests per batch; 0: 256 */
+    uint32_t inflight;         /* pipelines (batches in flight at once); 0: 2, at most 8 */
+    uint64_t staging_bytes;    /* page-locked image staging per pipeline; 0: 256 MiB.  A
+                                  request whose image is larger is read straight into
+                                  its host buffers */
+    uint64_t max_batch_tris;   /* input triangles per batch (the first request always
+                                  goes); 0: 1,000,000 */
 } rf_server_config;
 typedef struct {
     uint32_t ndraws;
@@ -371,10 +399,14 @@ typedef struct {
     int32_t status;            /* the request's own status */
     uint32_t batch_size;       /* requests in the batch it was rendered in */
     uint64_t batch_id;
-    double queue_ms;           /* submit -> its batch started */
-    double render_ms;          /* its batch: start -> rendered (GPU done) */
+    double queue_ms;           /* submit -> its batch was admitted */
+    double render_ms;          /* its batch on the GPU: gpu_end_ns - gpu_start_ns */
     double total_ms;           /* submit -> image in the host buffers */
     rf_stats stats;
+    uint64_t gpu_start_ns;     /* GPU global timer when its batch's work began on the */
+    uint64_t gpu_end_ns;       /* pipeline's stream, and when its rendering ended */
+    uint32_t pipeline;         /* the pipeline that rendered it */
+    uint32_t reserved_;
 } rf_result;
 rf_status rf_server_create(rf_ctx *ctx, const rf_server_config *cfg, rf_server **out);
 /* Queues a request; *ticket identifies it for rf_server_wait.  The host
@@ -386,6 +418,11 @@ rf_status rf_server_submit(rf_server *srv, const rf_request *req, uint64_t *tick
 rf_status rf_server_wait(rf_server *srv, uint64_t ticket, uint32_t timeout_ms, rf_result *out);
 /* Batches rendered, requests completed, requests queued right now. */
 rf_status rf_server_counts(rf_server *srv, uint64_t *batches, uint64_t *completed, uint64_t *queued);
+/* Admission charges of the batches in flight right now, the largest total
+ * seen so far (never above the budget unless one request alone was), and
+ * the most batches that were in flight at once.  NULL pointers are skipped. */
+rf_status rf_server_memory(rf_server *srv, uint64_t *charged, uint64_t *peak_charged,
+                           uint32_t *peak_inflight);
 rf_status rf_server_destroy(rf_server *srv);
 
 #ifdef __cplusplus

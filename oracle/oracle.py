@@ -25,7 +25,7 @@ class Draw(C.Structure):
 
 class Ctx(C.Structure):
     _fields_ = [("depth_test", C.c_int32), ("color_write", C.c_int32),
-                ("depth_write", C.c_int32), ("face_cull", C.c_int32)]
+                ("depth_write", C.c_int32), ("face_cull", C.c_int32), ("depth_sort", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -109,7 +109,7 @@ def render(draws, viewport, color, depth, ctx, pixfmt=0, stats=None):
     vp = np.ascontiguousarray(viewport, np.float32).reshape(-1)
     st = stats if stats is not None else Stats()
     c = Ctx(ctx.get("depth_test", 1), int(ctx.get("color_write", True)),
-            int(ctx.get("depth_write", True)), ctx.get("face_cull", 1))
+            int(ctx.get("depth_write", True)), ctx.get("face_cull", 1), ctx.get("depth_sort", 0))
     dp = _fp(depth) if depth is not None else C.POINTER(C.c_float)()
     for d in draws:
         L.rfo_render(C.byref(d), _fp(vp), _u32p(color), dp, w, h, pixfmt,
@@ -186,7 +186,7 @@ def render_lines(verts, lines, shader, viewport, color, depth, ctx, mvp=None, po
     vp = np.ascontiguousarray(viewport, np.float32).reshape(-1)
     st = stats if stats is not None else Stats()
     c = Ctx(ctx.get("depth_test", 1), int(ctx.get("color_write", True)),
-            int(ctx.get("depth_write", True)), ctx.get("face_cull", 1))
+            int(ctx.get("depth_write", True)), ctx.get("face_cull", 1), 0)
     dp = _fp(depth) if depth is not None else C.POINTER(C.c_float)()
     L.rfo_render_lines(C.byref(d), _u32p(li), li.size // 2, _fp(vp), _u32p(color), dp, w, h,
                        pixfmt, C.byref(c), C.byref(st))

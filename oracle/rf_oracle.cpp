@@ -12,7 +12,9 @@
 #include "rf_oracle.h"
 
 #include <cmath>
+#include <algorithm>
 #include <utility>
+#include <vector>
 #include <cstring>
 
 namespace {
@@ -425,17 +427,14 @@ void render_t(const rfo_draw *d, const float vp[16], uint32_t *color, float *dep
 
     // 2-4. Primitive assembly, clipping, then per clipped tri: to_screen,
     // face culling, tri_fill.  Clipped output order = input order with each
-    // clipped tri's fan in place (render.rs:167-205).
-    ClipVert<NA> clipped[POLY_CAP][3];
-    for (uint32_t t = 0; t < d->ntri; ++t) {
-        ClipVert<NA> tri[3];
-        for (int k = 0; k < 3; ++k) tri[k] = cv[d->idx[3 * t + k]];
-        int nc = clip_tri<NA>(tri, clipped);
-        for (int c = 0; c < nc; ++c) {
+    // clipped tri's fan in place (render.rs:167-205), optionally sorted by
+    // depth first (render.rs:180-182).
+    auto draw_clipped = [&](const ClipVert<NA> (&ct)[3]) {
+        {
             // prim.rs:62-88 to_screen.
             Var<NA> sv[3];
             for (int k = 0; k < 3; ++k) {
-                const ClipVert<NA> &v = clipped[c][k];
+                const ClipVert<NA> &v = ct[k];
                 float wv = v.pos[3];
                 const float ndc[4] = {v.pos[0] / wv, v.pos[1] / wv, 1.0f / wv, 1.0f};
                 sv[k].p[0] = dot4(vp + 0, ndc);  // Mat4 apply, mat.rs:945-949
@@ -454,7 +453,7 @@ void render_t(const rfo_draw *d, const float vp[16], uint32_t *color, float *dep
             // ctx.rs:95-101 face_cull.
             if ((ctx->face_cull == RFO_CULL_BACK && backface) ||
                 (ctx->face_cull == RFO_CULL_FRONT && !backface))
-                continue;
+                return;
             st->prims_o += 1;
             st->verts_o += 3;
 
@@ -506,6 +505,41 @@ void render_t(const rfo_draw *d, const float vp[16], uint32_t *color, float *dep
                 }
             }, [&] { st->oob += 1; });
         }
+    };
+    struct Clipped {
+        ClipVert<NA> v[3];
+    };
+    std::vector<Clipped> sorted;
+    ClipVert<NA> clipped[POLY_CAP][3];
+    for (uint32_t t = 0; t < d->ntri; ++t) {
+        ClipVert<NA> tri[3];
+        for (int k = 0; k < 3; ++k) tri[k] = cv[d->idx[3 * t + k]];
+        int nc = clip_tri<NA>(tri, clipped);
+        for (int c = 0; c < nc; ++c) {
+            if (ctx->depth_sort == RFO_SORT_NONE) {
+                draw_clipped(clipped[c]);
+            } else {
+                Clipped e;
+                for (int k = 0; k < 3; ++k) e.v[k] = clipped[c][k];
+                sorted.push_back(e);
+            }
+        }
+    }
+    if (ctx->depth_sort != RFO_SORT_NONE) {
+        // render.rs:209-219 depth_sort: key Render::depth = mean clip-space
+        // z (prim.rs:21-23), ordered by f32::total_cmp, ascending for
+        // FrontToBack and descending for BackToFront.  The reference's
+        // sort_unstable_by leaves equal keys in an unspecified order; this
+        // sort is stable (equal keys keep their submission and fan order).
+        auto depth = [](const Clipped &e) {
+            return (e.v[0].pos[2] + e.v[1].pos[2] + e.v[2].pos[2]) / 3.0f;
+        };
+        const bool back = ctx->depth_sort == RFO_SORT_BACK_TO_FRONT;
+        std::stable_sort(sorted.begin(), sorted.end(), [&](const Clipped &a, const Clipped &b) {
+            const int32_t ka = total_key(depth(a)), kb = total_key(depth(b));
+            return back ? kb < ka : ka < kb;
+        });
+        for (const Clipped &e : sorted) draw_clipped(e.v);
     }
     delete[] cv;
 }

@@ -53,11 +53,15 @@ typedef struct {
     int32_t sampler;
 } rfo_draw;
 
+/* Context::depth_sort: None / Some(FrontToBack) / Some(BackToFront). */
+enum { RFO_SORT_NONE = 0, RFO_SORT_FRONT_TO_BACK = 1, RFO_SORT_BACK_TO_FRONT = 2 };
+
 typedef struct {
     int32_t depth_test;
     int32_t color_write;
     int32_t depth_write;
     int32_t face_cull;
+    int32_t depth_sort;
 } rfo_ctx;
 
 typedef struct {

@@ -33,6 +33,8 @@ REPEAT_POT, CLAMP, ONCE = range(3)
 ARGB8888, XRGB8888, RGBA8888, BGRA8888 = range(4)
 DEPTH_NONE, DEPTH_LESS, DEPTH_EQUAL, DEPTH_GREATER = range(4)
 CULL_NONE, CULL_BACK, CULL_FRONT = range(3)
+# Context::depth_sort (ctx.rs:39): None, Some(FrontToBack), Some(BackToFront)
+SORT_NONE, SORT_FRONT_TO_BACK, SORT_BACK_TO_FRONT = range(3)
 NATTR = {FLAT: 0, GOURAUD: 3, TEXTURED: 2, TEX_GOURAUD: 5, GOURAUD_SRGB: 3}
 
 STAGES = ("vertex", "clip", "scan", "setup", "raster")
@@ -56,7 +58,7 @@ class Uniforms(C.Structure):
 
 class Flags(C.Structure):
     _fields_ = [("depth_test", C.c_int32), ("color_write", C.c_int32),
-                ("depth_write", C.c_int32), ("face_cull", C.c_int32)]
+                ("depth_write", C.c_int32), ("face_cull", C.c_int32), ("depth_sort", C.c_int32)]
 
 
 class CStats(C.Structure):
@@ -80,7 +82,8 @@ class Job(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch", C.c_uint32),
-                ("reserved_", C.c_uint32)]
+                ("inflight", C.c_uint32), ("staging_bytes", C.c_uint64),
+                ("max_batch_tris", C.c_uint64)]
 
 
 class Request(C.Structure):
@@ -93,7 +96,8 @@ class Request(C.Structure):
 class Result(C.Structure):
     _fields_ = [("status", C.c_int32), ("batch_size", C.c_uint32), ("batch_id", C.c_uint64),
                 ("queue_ms", C.c_double), ("render_ms", C.c_double), ("total_ms", C.c_double),
-                ("stats", CStats)]
+                ("stats", CStats), ("gpu_start_ns", C.c_uint64), ("gpu_end_ns", C.c_uint64),
+                ("pipeline", C.c_uint32), ("reserved_", C.c_uint32)]
 
 
 # Exported symbols of include/rfgpu.h with their ctypes signatures.
@@ -140,6 +144,7 @@ _SIGS = {
     "rf_server_wait": [_P, C.c_uint64, C.c_uint32, C.POINTER(Result)],
     "rf_server_counts": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
     "rf_server_destroy": [_P],
+    "rf_server_memory": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)],
     "rf_obj_parse": [C.c_char_p, C.c_size_t, C.c_int32, C.POINTER(C.POINTER(C.c_float)),
                      C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_uint32)),
                      C.POINTER(C.c_uint32), C.c_char_p, C.c_size_t],
@@ -223,10 +228,8 @@ class Context:
     """Context (ctx.rs:11-126); defaults equal Context::default()."""
 
     def __init__(self, color_clear=0xFF000000, depth_clear=float("inf"), face_cull=CULL_BACK,
-                 depth_test=DEPTH_LESS, color_write=True, depth_write=True, depth_sort=None):
-        if depth_sort is not None:
-            raise NotImplementedError("depth_sort: the reference's unstable sort has no "
-                                      "defined order for equal depths")
+                 depth_test=DEPTH_LESS, color_write=True, depth_write=True, depth_sort=SORT_NONE):
+        self.depth_sort = SORT_NONE if depth_sort is None else depth_sort  # SORT_*
         self.color_clear = color_clear    # Color4 as r|g<<8|b<<16|a<<24, or None
         self.depth_clear = depth_clear    # f32 or None
         self.face_cull = face_cull
@@ -237,7 +240,7 @@ class Context:
 
     def flags(self):
         return Flags(self.depth_test, int(bool(self.color_write)), int(bool(self.depth_write)),
-                     self.face_cull)
+                     self.face_cull, self.depth_sort)
 
 
 class Device:
@@ -626,25 +629,30 @@ def autotune(scenes, reps=3, device=None):
 
 
 class Server:
-    """rf_server: a worker thread that owns the device context and renders
-    queued requests in continuous batches under a device-memory budget.
-    While it runs, make no other call on that Device."""
+    """rf_server: continuous batching over `inflight` pipelines (worker
+    threads with their own streams) that read the device context's meshes
+    and textures, under a device-memory budget.  While it runs, make no
+    other call on that Device."""
 
     WAIT_FOREVER = 0xFFFFFFFF
 
-    def __init__(self, device, hbm_budget_bytes=0, max_batch=0):
+    def __init__(self, device, hbm_budget_bytes=0, max_batch=0, inflight=0, staging_bytes=0,
+                 max_batch_tris=0):
         self.dev = device
-        cfg = ServerConfig(hbm_budget_bytes, max_batch, 0)
+        cfg = ServerConfig(hbm_budget_bytes, max_batch, inflight, staging_bytes, max_batch_tris)
         p = _P()
         _check(lib().rf_server_create(device.ptr, C.byref(cfg), C.byref(p)), "rf_server_create")
         self.ptr = p
         self._keep = {}
 
     def submit(self, draws, to_screen, w, h, ctx=None, pixfmt=ARGB8888, depth=True,
-               color_out=None, depth_out=None):
+               color_out=None, depth_out=None, read_depth=None):
         """Queue a scene; returns a ticket.  draws: list of (Mesh, Shader,
-        mvp).  color_out / depth_out: (h, w) uint32 / float32 host arrays
-        that receive the image (allocated here when None)."""
+        mvp).  depth: the target has a depth buffer (Framebuf) or not
+        (Colorbuf); read_depth (default: depth) copies it out too.
+        color_out / depth_out: (h, w) uint32 / float32 host arrays that
+        receive the image (allocated here when None)."""
+        read_depth = depth if read_depth is None else (read_depth and depth)
         ctx = ctx or Context()
         arr = (Draw * max(1, len(draws)))()
         for i, dr in enumerate(draws):
@@ -655,7 +663,7 @@ class Server:
             arr[i].uniforms = shader.uniforms(mvp)
         if color_out is None:
             color_out = np.empty((h, w), np.uint32)
-        if depth and depth_out is None:
+        if read_depth and depth_out is None:
             depth_out = np.empty((h, w), np.float32)
         q = Request()
         q.ndraws = len(draws)
@@ -667,10 +675,10 @@ class Server:
         q.clear_rgba = cc
         q.depth_clear = float("inf") if ctx.depth_clear is None else ctx.depth_clear
         q.color_out = _u32p(color_out)
-        q.depth_out = _fp(depth_out) if depth else None
+        q.depth_out = _fp(depth_out) if read_depth else None
         t = C.c_uint64()
         _check(lib().rf_server_submit(self.ptr, C.byref(q), C.byref(t)), "rf_server_submit")
-        self._keep[t.value] = (color_out, depth_out if depth else None)
+        self._keep[t.value] = (color_out, depth_out if read_depth else None)
         return t.value
 
     def wait(self, ticket, timeout_ms=WAIT_FOREVER):
@@ -681,7 +689,8 @@ class Server:
         col, dep = self._keep.pop(ticket)
         res = {"status": r.status, "batch_size": r.batch_size, "batch_id": r.batch_id,
                "queue_ms": r.queue_ms, "render_ms": r.render_ms, "total_ms": r.total_ms,
-               "stats": Stats.from_c(r.stats)}
+               "stats": Stats.from_c(r.stats), "gpu_start_ns": r.gpu_start_ns,
+               "gpu_end_ns": r.gpu_end_ns, "pipeline": r.pipeline}
         return col, dep, res
 
     def counts(self):
@@ -689,6 +698,14 @@ class Server:
         _check(lib().rf_server_counts(self.ptr, C.byref(b), C.byref(c), C.byref(q)),
                "rf_server_counts")
         return {"batches": b.value, "completed": c.value, "queued": q.value}
+
+    def memory(self):
+        """Admission charges in flight now, their peak, and the most batches
+        in flight at once."""
+        c, pk, pi = C.c_uint64(), C.c_uint64(), C.c_uint32()
+        _check(lib().rf_server_memory(self.ptr, C.byref(c), C.byref(pk), C.byref(pi)),
+               "rf_server_memory")
+        return {"charged": c.value, "peak_charged": pk.value, "peak_inflight": pi.value}
 
     def close(self):
         if self.ptr:

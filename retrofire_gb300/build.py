@@ -13,9 +13,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "librfgpu.so")
-SRCS = ["rf_kernels.cu", "rf_api.cu", "rf_noalloc.cu", "rf_server.cu", "rf_obj.cu", "rf_lines.cu", "rf_raster_tw8.cu", "rf_raster_tw16.cu",
+SRCS = ["rf_kernels.cu", "rf_sort.cu", "rf_api.cu", "rf_noalloc.cu", "rf_server.cu", "rf_obj.cu", "rf_lines.cu", "rf_raster_tw8.cu", "rf_raster_tw16.cu",
         "rf_raster_tw32.cu", "rf_raster_tw64.cu"]
-HDRS = ["rf_exact.cuh", "rf_internal.cuh", "rf_kernels.cuh", "rf_device.cuh", "rf_raster.cuh"]
+HDRS = ["rf_exact.cuh", "rf_internal.cuh", "rf_kernels.cuh", "rf_device.cuh", "rf_raster.cuh",
+        "rf_ctx_internal.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
          "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/rfgpu.h"
+#include "rf_ctx_internal.h"
 #include "rf_internal.cuh"
 #include "rf_kernels.cuh"
 
@@ -66,6 +67,12 @@ struct Target {
     cudaEvent_t rendered = nullptr, read_done = nullptr;
 };
 
+// Mesh and texture tables by handle.
+struct Resources {
+    std::unordered_map<uint64_t, Mesh> meshes;
+    std::unordered_map<uint64_t, Texture> textures;
+};
+
 // Grow-only device buffer.
 struct DevBuf {
     void *p = nullptr;
@@ -88,7 +95,7 @@ constexpr size_t RF_GRAPH_CACHE = 8;
 // one timed frame per tile width in RF_TUNE_TW, then the fastest width for
 // every later frame of that shape.  All widths give identical results.
 constexpr uint32_t RF_TUNE_TW[4] = {8, 16, 32, 64};
-constexpr size_t RF_TUNE_CACHE = 32;
+constexpr size_t RF_TUNE_CACHE = 512;  // frame shapes remembered (a per-frame loop over a few hundred scenes)
 struct TuneState {
     uint64_t key[5];
     uint32_t next = 0;  // 0: warm-up, 1..4: timed RF_TUNE_TW[next-1], 5: decided
@@ -111,13 +118,22 @@ struct rf_ctx {
     int device = 0;
     uint32_t tile_w = 32, warps = 4;
     uint64_t next_handle = 1;
-    std::unordered_map<uint64_t, Mesh> meshes;
-    std::unordered_map<uint64_t, Texture> textures;
+    // Meshes and textures: the context's own tables, or (a context made by
+    // rfi_ctx_share for the serving loop) those of the context it shares
+    // them with, read-only while shared.
+    Resources own_res;
+    Resources *res = &own_res;
+    bool shared_res = false;
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
     DevBuf triw, trib, scan64, rowtot, rows, rprims, live, marks, items, jstats;
     DevBuf lrec, lmask;  // line pass
+    // depth-sorted frames: sorted order, source triangles, per-draw counts,
+    // sort scratch, the setup pass's draws / jobs, the raster's unit arrays
+    DevBuf perm, ptri, nout, dsort, vdraws, vjobs, vtoff, vtcnt;
+    uint32_t *nout_host = nullptr;  // pinned, grown with the draw count
+    size_t nout_host_cap = 0;
     // CUDA graphs of the launch sequence, keyed by frame shape (graph mode).
     bool graphs = false;
     uint64_t gen = 0;  // bumped whenever a scratch buffer moves
@@ -329,14 +345,12 @@ struct JobIn {
 
 // Host-side counts of one job (render.rs:152-155) and its slot among the
 // jobs that reach the GPU (-1: no triangles).
-struct JobHost {
-    uint64_t calls = 0, prims_i = 0, verts_i = 0;
-    int32_t slot = -1;
-};
+using JobHost = rfi_counts;
 
 bool flags_ok(const rf_context_flags *fl) {
     return fl && fl->depth_test >= RF_DEPTH_NONE && fl->depth_test <= RF_DEPTH_GREATER &&
-           fl->face_cull >= RF_CULL_NONE && fl->face_cull <= RF_CULL_FRONT;
+           fl->face_cull >= RF_CULL_NONE && fl->face_cull <= RF_CULL_FRONT &&
+           fl->depth_sort >= RF_SORT_NONE && fl->depth_sort <= RF_SORT_BACK_TO_FRONT;
 }
 
 void graphs_drop(rf_ctx *ctx) {
@@ -380,11 +394,12 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
         const uint64_t nt0 = nt, nv0 = nv;
         for (uint32_t i = 0; i < ji.ndraws; ++i) {
             const rf_draw &dr = ji.draws[i];
-            auto mit = ctx->meshes.find(dr.mesh);
-            if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+            auto mit = ctx->res->meshes.find(dr.mesh);
+            if (mit == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
             Mesh &m = mit->second;
             if (m.lines) return RF_ERR_BAD_ARG;  // line meshes render with rf_render_lines
-            if (m.async && (ctx->async_meshes.empty() || ctx->async_meshes.back() != &m))
+            if (m.async && !ctx->shared_res &&
+                (ctx->async_meshes.empty() || ctx->async_meshes.back() != &m))
                 ctx->async_meshes.push_back(&m);
             if (dr.shader < RF_SHADER_FLAT || dr.shader > RF_SHADER_GOURAUD_SRGB) return RF_ERR_BAD_ARG;
             if (m.nattr != nattr_for(dr.shader)) return RF_ERR_BAD_ARG;
@@ -400,8 +415,8 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
             d.sampler = (int32_t)dr.uniforms.sampler;
             d.flat_rgba = dr.uniforms.flat_rgba;
             if (dr.shader == RF_SHADER_TEXTURED || dr.shader == RF_SHADER_TEX_GOURAUD) {
-                auto tit = ctx->textures.find(dr.uniforms.texture);
-                if (tit == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+                auto tit = ctx->res->textures.find(dr.uniforms.texture);
+                if (tit == ctx->res->textures.end()) return RF_ERR_BAD_HANDLE;
                 if (d.sampler < RF_SAMPLER_REPEAT_POT || d.sampler > RF_SAMPLER_ONCE) return RF_ERR_BAD_ARG;
                 if (d.sampler == RF_SAMPLER_REPEAT_POT && (!is_pot(tit->second.w) || !is_pot(tit->second.h)))
                     return RF_ERR_NON_POT_TEXTURE;
@@ -414,6 +429,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
             d.job = (uint32_t)hj.size();
             d.flags = dr.flags & RF_DRAW_CULL_BBOX;
             d.culled = 0;
+            d.src_tri_base = (uint32_t)nt;
             memcpy(d.bbox, m.bbox, sizeof d.bbox);
             memcpy(d.mvp, dr.uniforms.mvp, sizeof d.mvp);
             nv += m.nverts;
@@ -453,6 +469,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
         J.clear_flags = tg.clear_flags;
         J.clear_px = tg.clear_px;
         J.clear_z = tg.clear_z;
+        J.depth_sort = ji.fl->depth_sort;
         memcpy(J.vp, ji.vp, sizeof J.vp);
         tiles += (uint64_t)J.tiles_x * J.tiles_y;
         mask_words += (uint64_t)J.tiles_x * J.tiles_y * J.mask_words;
@@ -685,8 +702,119 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         return RF_OK;
     };
 
+    // A frame with depth-sorted jobs (render.rs:180-182): vertex, clip and
+    // the scan as usual; then the clipped triangles' count per draw comes
+    // back to the host (one wait), the triangles are sorted on the device
+    // (rf_sort.cu), and setup, binning and the raster pass run over the
+    // sorted order, every clipped triangle one unit of the tile masks.
+    bool sorted = false;
+    for (const JobDev &J : hj) sorted = sorted || J.depth_sort != RF_SORT_NONE;
+    uint64_t sort_kernels = 0;
+    auto enqueue_sorted = [&]() -> rf_status {
+        auto mark = [&](int i) -> cudaError_t { return ctx->timing ? cudaEventRecord(ev[i], s) : cudaSuccess; };
+        if (per_job) CK(cudaMemsetAsync(kst, 0, nj * sizeof(StatsDev), s));
+        CK(mark(RF_STAGE_VERTEX));
+        if (any_cull) CK(rfk::launch_cull(P<DrawDev>(ctx->draws), ndraws, kst, ctx->nsm, s));
+        CK(rfk::launch_vertex(dd, ndraws, (uint32_t)nv, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                              counters, P<unsigned long long>(ctx->marks), ctx->nsm, s));
+        CK(mark(RF_STAGE_CLIP));
+        CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
+                            P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<uint32_t>(ctx->toff),
+                            P<PolyVert>(ctx->pool), pool_cap, counters, ctx->nsm, s));
+        CK(mark(RF_STAGE_SCAN));
+        CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
+                            P<uint32_t>(ctx->scan), counters + RF_CNT_PRIMS, s));
+        rf_status st2;
+        if ((st2 = ensure(ctx, ctx->nout, (size_t)ndraws * 4))) return st2;
+        CK(rfk::launch_draw_counts(dd, ndraws, (uint32_t)nt, P<uint32_t>(ctx->toff), counters,
+                                   P<uint32_t>(ctx->nout), s));
+        if (ctx->nout_host_cap < ndraws) {
+            CK(cudaStreamSynchronize(s));
+            if (ctx->nout_host) CK(cudaFreeHost(ctx->nout_host));
+            ctx->nout_host = nullptr;
+            ctx->nout_host_cap = 0;
+            CK(cudaMallocHost(&ctx->nout_host, (size_t)ndraws * 4));
+            ctx->nout_host_cap = ndraws;
+        }
+        CK(cudaMemcpyAsync(ctx->nout_host, ctx->nout.p, (size_t)ndraws * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        // The setup pass's draws and jobs count clipped triangles, in the
+        // sorted order (draw by draw, as the keys lead with the draw).
+        std::vector<DrawDev> vd = hd;
+        std::vector<JobDev> vj = hj;
+        uint64_t np = 0;
+        for (uint32_t d = 0; d < ndraws; ++d) {
+            vd[d].tri_base = (uint32_t)np;
+            vd[d].ntri = ctx->nout_host[d];
+            np += ctx->nout_host[d];
+        }
+        if (np > 0x7FFFFFF0ull) return RF_ERR_BAD_ARG;
+        for (JobDev &J : vj) {
+            J.ntri = 0;
+            J.tri_base = 0;
+        }
+        for (int64_t d = (int64_t)ndraws - 1; d >= 0; --d) {  // each job's first draw sets its base
+            JobDev &J = vj[vd[d].job];
+            J.tri_base = vd[d].tri_base;
+            J.ntri += vd[d].ntri;
+        }
+        for (JobDev &J : vj) J.mask_words = (J.ntri + 31) / 32;
+        layout_masks(vj);
+        const size_t vmask = vj.back().sum_base + (size_t)vj.back().tiles_x * vj.back().tiles_y * vj.back().sum_words;
+        const uint32_t n32 = (uint32_t)np;
+        if ((st2 = ensure(ctx, ctx->mask, std::max<size_t>(vmask, 1) * 4))) return st2;
+        if ((st2 = ensure(ctx, ctx->perm, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
+        if ((st2 = ensure(ctx, ctx->ptri, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
+        if ((st2 = ensure(ctx, ctx->dsort, rfk::dsort_scratch_bytes(n32)))) return st2;
+        if ((st2 = ensure(ctx, ctx->scan,
+                          rfk::scan_scratch_words(std::max<uint32_t>(rfk::dsort_scan_items(n32), (uint32_t)nt)) * 4)))
+            return st2;
+        if ((st2 = ensure(ctx, ctx->triw, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
+        if ((st2 = ensure(ctx, ctx->trib, (size_t)std::max<uint32_t>(n32, 1) * 8))) return st2;
+        if ((st2 = ensure(ctx, ctx->scan64, rfk::scan64_scratch_words(n32) * 8))) return st2;
+        if ((st2 = ensure(ctx, ctx->vtoff, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
+        if ((st2 = ensure(ctx, ctx->vtcnt, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
+        if ((st2 = ensure(ctx, ctx->vdraws, vd.size() * sizeof(DrawDev)))) return st2;
+        if ((st2 = ensure(ctx, ctx->vjobs, vj.size() * sizeof(JobDev)))) return st2;
+        CK(cudaMemcpyAsync(ctx->vdraws.p, vd.data(), vd.size() * sizeof(DrawDev), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->vjobs.p, vj.data(), vj.size() * sizeof(JobDev), cudaMemcpyHostToDevice, s));
+        const DrawDev *vdd = P<DrawDev>(ctx->vdraws);
+        const JobDev *vjd = P<JobDev>(ctx->vjobs);
+        CK(mark(RF_STAGE_SETUP));
+        CK(rfk::launch_dsort(dd, ndraws, jd, (uint32_t)nt, n32, P<float4>(ctx->cpos), P<uint32_t>(ctx->tcnt),
+                             P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
+                             counters, P<uint32_t>(ctx->perm), P<uint32_t>(ctx->ptri), ctx->dsort.p,
+                             P<uint32_t>(ctx->scan), s));
+        CK(cudaMemsetAsync(ctx->mask.p, 0, vmask * 4, s));
+        CK(rfk::launch_iota(P<uint32_t>(ctx->vtoff), P<uint32_t>(ctx->vtcnt), n32, s));
+        CK(rfk::launch_setup(vdd, ndraws, vjd, n32, TW, P<float4>(ctx->cpos), P<uint32_t>(ctx->tcnt),
+                             P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
+                             P<PrimRec>(ctx->prims), P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
+                             P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
+                             P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
+                             P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
+                             kst, counters, ctx->nsm, s, P<uint32_t>(ctx->perm), P<uint32_t>(ctx->ptri)));
+        CK(rfk::launch_items(vjd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
+                             (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));
+        CK(mark(RF_STAGE_RASTER));
+        CK(rfk::launch_raster(TW, kind, fast, vjd, nj, vdd, P<PrimRec>(ctx->prims), P<RasterPrim>(ctx->rprims),
+                              P<uint32_t>(ctx->rows), P<uint32_t>(ctx->vtcnt), P<uint32_t>(ctx->vtoff),
+                              P<uint32_t>(ctx->mask), ntiles, P<uint32_t>(ctx->items), counters + RF_CNT_ITEMS,
+                              counters + RF_CNT_QUEUE, kst, ctx->warps, ctx->nsm, s));
+        CK(mark(RF_STAGE_N));
+        if (per_job) CK(rfk::launch_stats_fold(kst, nj, P<StatsDev>(ctx->stats), s));
+        // draw counts, sort keys, per digit pass a histogram, a scan of 1 or 3
+        // launches and a scatter, the unit arrays
+        const uint32_t dpasses = 4 + (ndraws > 1 ? (ndraws > 256 ? (ndraws > 65536 ? 3 : 2) : 1) : 0);
+        const uint32_t sitems = rfk::dsort_scan_items(n32);
+        sort_kernels = 2 + (n32 ? 1 + dpasses * (2 + (sitems <= RF_SCAN_BLOCK_ITEMS ? 1 : 3)) + 1 : 0);
+        return RF_OK;
+    };
+
     if (tuned) CK(cudaEventRecord(tuned->e0, s));
-    if (ctx->graphs && !ctx->timing) {
+    if (sorted) {
+        if ((st = enqueue_sorted())) return st;
+    } else if (ctx->graphs && !ctx->timing) {
         GraphKey key{};
         const uint64_t kv[] = {ctx->gen, ndraws, nj, nv, nt, ntiles, mask_words, TW, ctx->warps,
                                (uint64_t)(kind + 16) | (any_cull ? 0x100u : 0u), fast ? 1u : 0u,
@@ -732,7 +860,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     }
     // vertex, clip (2), scan (3, or 1 for one block), setup, scan64 (the same),
     // bin, work list, raster (+ the stats fold)
-    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 9 : 13) + (per_job ? 1 : 0) + (any_cull ? 1 : 0);
+    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 9 : 13) + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -789,9 +917,28 @@ rf_status upload_mesh(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t
     }
     mesh_bbox(m, verts);
     const uint64_t h = ctx->next_handle++;
-    ctx->meshes[h] = m;
+    ctx->res->meshes[h] = m;
     *out = h;
     return RF_OK;
+}
+
+// The jobs of a batch (distinct targets of this context) queued as one pass.
+rf_status queue_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, std::vector<JobHost> &host) {
+    std::vector<JobIn> in(njobs);
+    std::vector<rf_target> seen(njobs);
+    for (uint32_t k = 0; k < njobs; ++k) {
+        auto it = ctx->targets.find(jobs[k].target);
+        if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
+        in[k].draws = jobs[k].draws;
+        in[k].ndraws = jobs[k].ndraws;
+        in[k].vp = jobs[k].viewport;
+        in[k].tg = &it->second;
+        in[k].fl = &jobs[k].flags;
+        seen[k] = jobs[k].target;
+    }
+    std::sort(seen.begin(), seen.end());
+    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return RF_ERR_BAD_ARG;
+    return run_jobs(ctx, in.data(), njobs, true, host);
 }
 
 rf_status finish_call(rf_ctx *ctx, rf_stats *out) {
@@ -863,8 +1010,10 @@ rf_status rf_ctx_create(void *cuda_stream, rf_ctx **out) {
 rf_status rf_ctx_destroy(rf_ctx *ctx) {
     if (!ctx) return RF_ERR_BAD_ARG;
     sync_all(ctx);
-    for (auto &kv : ctx->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); drop_async(kv.second); }
-    for (auto &kv : ctx->textures) cudaFree(kv.second.texels);
+    if (!ctx->shared_res) {
+        for (auto &kv : ctx->res->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); drop_async(kv.second); }
+        for (auto &kv : ctx->res->textures) cudaFree(kv.second.texels);
+    }
     for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); drop_async(kv.second); }
     if (ctx->up) cudaStreamDestroy(ctx->up);
     if (ctx->down) cudaStreamDestroy(ctx->down);
@@ -876,7 +1025,10 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
-                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->marks, &ctx->items, &ctx->jstats, &ctx->lrec, &ctx->lmask};
+                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->marks, &ctx->items, &ctx->jstats, &ctx->lrec, &ctx->lmask,
+                      &ctx->perm, &ctx->ptri, &ctx->nout, &ctx->dsort, &ctx->vdraws, &ctx->vjobs,
+                      &ctx->vtoff, &ctx->vtcnt};
+    if (ctx->nout_host) cudaFreeHost(ctx->nout_host);
     if (ctx->rows_need_host) cudaFreeHost(ctx->rows_need_host);
     if (ctx->rows_evt) cudaEventDestroy(ctx->rows_evt);
     for (DevBuf *b : bufs) cudaFree(b->p);
@@ -975,8 +1127,8 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
                           const float viewport[16], rf_target target, const rf_context_flags *fl,
                           rf_stats *stats) {
     if (!ctx || !u || !viewport || !flags_ok(fl)) return RF_ERR_BAD_ARG;
-    auto mit = ctx->meshes.find(mesh);
-    if (mit == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    auto mit = ctx->res->meshes.find(mesh);
+    if (mit == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     auto tit = ctx->targets.find(target);
     if (tit == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = mit->second;
@@ -998,8 +1150,8 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
     d.sampler = (int32_t)u->sampler;
     d.flat_rgba = u->flat_rgba;
     if (shader == RF_SHADER_TEXTURED || shader == RF_SHADER_TEX_GOURAUD) {
-        auto xit = ctx->textures.find(u->texture);
-        if (xit == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+        auto xit = ctx->res->textures.find(u->texture);
+        if (xit == ctx->res->textures.end()) return RF_ERR_BAD_HANDLE;
         if (d.sampler < RF_SAMPLER_REPEAT_POT || d.sampler > RF_SAMPLER_ONCE) return RF_ERR_BAD_ARG;
         if (d.sampler == RF_SAMPLER_REPEAT_POT && (!is_pot(xit->second.w) || !is_pot(xit->second.h)))
             return RF_ERR_NON_POT_TEXTURE;
@@ -1059,8 +1211,8 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
 
 rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    auto it = ctx->meshes.find(mesh);
-    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    auto it = ctx->res->meshes.find(mesh);
+    if (it == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = it->second;
     const uint32_t per = m.lines ? 2u : 3u;
     if (idx)
@@ -1078,8 +1230,8 @@ rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const ui
 
 rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    auto it = ctx->meshes.find(mesh);
-    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    auto it = ctx->res->meshes.find(mesh);
+    if (it == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = it->second;
     const uint32_t per = m.lines ? 2u : 3u;
     if (idx)
@@ -1101,8 +1253,8 @@ rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, co
 
 rf_status rf_mesh_info(rf_ctx *ctx, rf_mesh mesh, uint32_t *nverts, uint32_t *ntri, uint32_t *nattr) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    auto it = ctx->meshes.find(mesh);
-    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    auto it = ctx->res->meshes.find(mesh);
+    if (it == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     if (nverts) *nverts = it->second.nverts;
     if (ntri) *ntri = it->second.ntri;
     if (nattr) *nattr = it->second.nattr;
@@ -1111,14 +1263,14 @@ rf_status rf_mesh_info(rf_ctx *ctx, rf_mesh mesh, uint32_t *nverts, uint32_t *nt
 
 rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    auto it = ctx->meshes.find(mesh);
-    if (it == ctx->meshes.end()) return RF_ERR_BAD_HANDLE;
+    auto it = ctx->res->meshes.find(mesh);
+    if (it == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     rf_status st = sync_all(ctx);
     if (st) return st;
     cudaFree(it->second.verts);
     cudaFree(it->second.idx);
     drop_async(it->second);
-    ctx->meshes.erase(it);
+    ctx->res->meshes.erase(it);
     return RF_OK;
 }
 
@@ -1137,18 +1289,18 @@ rf_status rf_texture_upload(rf_ctx *ctx, const uint32_t *rgba, uint32_t w, uint3
         return cuda_fail(ctx, e, "rf_texture_upload");
     }
     const uint64_t hd = ctx->next_handle++;
-    ctx->textures[hd] = t;
+    ctx->res->textures[hd] = t;
     *out = hd;
     return RF_OK;
 }
 
 rf_status rf_texture_destroy(rf_ctx *ctx, rf_texture tex) {
     if (!ctx) return RF_ERR_BAD_ARG;
-    auto it = ctx->textures.find(tex);
-    if (it == ctx->textures.end()) return RF_ERR_BAD_HANDLE;
+    auto it = ctx->res->textures.find(tex);
+    if (it == ctx->res->textures.end()) return RF_ERR_BAD_HANDLE;
     CK(cudaStreamSynchronize(ctx->stream));
     cudaFree(it->second.texels);
-    ctx->textures.erase(it);
+    ctx->res->textures.erase(it);
     return RF_OK;
 }
 
@@ -1288,22 +1440,8 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
 
 rf_status rf_render_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, rf_stats *stats) {
     if (!ctx || (njobs && !jobs)) return RF_ERR_BAD_ARG;
-    std::vector<JobIn> in(njobs);
-    std::vector<rf_target> seen(njobs);
-    for (uint32_t k = 0; k < njobs; ++k) {
-        auto it = ctx->targets.find(jobs[k].target);
-        if (it == ctx->targets.end()) return RF_ERR_BAD_HANDLE;
-        in[k].draws = jobs[k].draws;
-        in[k].ndraws = jobs[k].ndraws;
-        in[k].vp = jobs[k].viewport;
-        in[k].tg = &it->second;
-        in[k].fl = &jobs[k].flags;
-        seen[k] = jobs[k].target;
-    }
-    std::sort(seen.begin(), seen.end());
-    if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return RF_ERR_BAD_ARG;
     std::vector<JobHost> host;
-    rf_status st = run_jobs(ctx, in.data(), njobs, true, host);
+    rf_status st = queue_batch(ctx, jobs, njobs, host);
     if (st) return st;
     if (!stats) return RF_OK;
     // Per-job stats: this batch's slots plus the host counts; the running
@@ -1313,27 +1451,8 @@ rf_status rf_render_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, rf_st
     CK(cudaStreamSynchronize(ctx->stream));
     if (!js.empty())
         CK(cudaMemcpy(js.data(), ctx->jstats.p, js.size() * sizeof(StatsDev), cudaMemcpyDeviceToHost));
-    for (uint32_t k = 0; k < njobs; ++k) {
-        rf_stats o{};
-        o.calls = host[k].calls;
-        o.prims_i = host[k].prims_i;
-        o.verts_i = host[k].verts_i;
-        if (host[k].slot >= 0) {
-            const StatsDev &d = js[host[k].slot];
-            o.prims_o = d.prims_o;
-            o.verts_o = d.verts_o;
-            o.frags_i = d.frags_i;
-            o.frags_o = d.frags_o;
-            o.oob = d.oob;
-            o.calls -= d.cull_calls;
-            o.prims_i -= d.cull_prims;
-            o.verts_i -= d.cull_verts;
-            o.objs_i = d.objs_i;
-            o.objs_o = d.objs_o;
-        }
-        stats[k] = o;
-        add_stats(ctx->taken, o);
-    }
+    rfi_batch_stats(host, js.data(), stats);
+    for (uint32_t k = 0; k < njobs; ++k) add_stats(ctx->taken, stats[k]);
     return RF_OK;
 }
 
@@ -1482,3 +1601,76 @@ rf_status rf_ctx_autotune(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, uint3
 }
 
 }  // extern "C"
+
+// ---- internal interface of the serving loop (rf_ctx_internal.h) --------
+
+void rfi_batch_stats(const std::vector<rfi_counts> &counts, const StatsDev *js, rf_stats *out) {
+    for (size_t k = 0; k < counts.size(); ++k) {
+        rf_stats o{};
+        o.calls = counts[k].calls;
+        o.prims_i = counts[k].prims_i;
+        o.verts_i = counts[k].verts_i;
+        if (counts[k].slot >= 0) {
+            const StatsDev &d = js[counts[k].slot];
+            o.prims_o = d.prims_o;
+            o.verts_o = d.verts_o;
+            o.frags_i = d.frags_i;
+            o.frags_o = d.frags_o;
+            o.oob = d.oob;
+            o.calls -= d.cull_calls;
+            o.prims_i -= d.cull_prims;
+            o.verts_i -= d.cull_verts;
+            o.objs_i = d.objs_i;
+            o.objs_o = d.objs_o;
+        }
+        out[k] = o;
+    }
+}
+
+rf_status rfi_ctx_share(rf_ctx *parent, rf_ctx **out) {
+    if (!parent || !out) return RF_ERR_BAD_ARG;
+    *out = nullptr;
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+        cudaGetLastError();
+        return RF_ERR_CUDA;
+    }
+    if (prev != parent->device && cudaSetDevice(parent->device) != cudaSuccess) {
+        cudaGetLastError();
+        return RF_ERR_CUDA;
+    }
+    rf_ctx *ctx = nullptr;
+    rf_status st = rf_ctx_create(nullptr, &ctx);
+    if (prev != parent->device) cudaSetDevice(prev);
+    if (st) return st;
+    ctx->res = parent->res;
+    ctx->shared_res = true;
+    ctx->tile_w = parent->tile_w;
+    ctx->warps = parent->warps;
+    ctx->tune_online = parent->tune_online;
+    *out = ctx;
+    return RF_OK;
+}
+
+cudaStream_t rfi_ctx_stream(rf_ctx *ctx) { return ctx ? ctx->stream : nullptr; }
+
+rf_status rfi_render_batch_async(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, StatsDev *js_host,
+                                 uint32_t js_cap, std::vector<rfi_counts> &counts) {
+    if (!ctx || (njobs && !jobs) || njobs > js_cap || (njobs && !js_host)) return RF_ERR_BAD_ARG;
+    rf_status st = queue_batch(ctx, jobs, njobs, counts);
+    if (st) return st;
+    const size_t n = ctx->hjobs.size();  // jobs that reached the GPU (this batch)
+    bool any = false;
+    for (const rfi_counts &c : counts) any = any || c.slot >= 0;
+    if (any && n)
+        CK(cudaMemcpyAsync(js_host, ctx->jstats.p, n * sizeof(StatsDev), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    return RF_OK;
+}
+
+rf_status rfi_stamp(rf_ctx *ctx, unsigned long long *dst) {
+    if (!ctx || !dst) return RF_ERR_BAD_ARG;
+    CK(rfk::launch_stamp(dst, ctx->stream));
+    ctx->kernels += 1;
+    return RF_OK;
+}

@@ -36,6 +36,9 @@ struct DrawDev {
     uint32_t job;
     uint32_t flags;   // RF_DRAW_CULL_BBOX
     uint32_t culled;  // set on the device: the draw's bbox is Hidden
+    uint32_t src_tri_base;  // first global input triangle (== tri_base except in a
+                            // depth-sorted frame's setup, where tri_base counts
+                            // clipped triangles)
     float bbox[6];    // BBox::of the positions: low x,y,z, high x,y,z
     float mvp[16];
 };
@@ -54,6 +57,7 @@ struct JobDev {
     uint32_t clear_px;
     float clear_z;
     uint32_t sum_words;       // summary words per tile: bit b of word s = mask word 32 s + b is nonzero
+    int32_t depth_sort;       // Context::depth_sort: 0 none, 1 front to back, 2 back to front
     uint64_t sum_base;        // word offset of the job's tile-0 summary (after every job's masks)
     float vp[16];             // Mat4<Ndc, Screen>
 };

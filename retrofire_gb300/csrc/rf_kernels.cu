@@ -697,7 +697,8 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
                         uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
                         uint32_t *__restrict__ live, uint32_t *__restrict__ live_n,
-                        uint32_t *__restrict__ extra, StatsDev *__restrict__ stats) {
+                        uint32_t *__restrict__ extra, StatsDev *__restrict__ stats,
+                        const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ptri) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *extra = 0;  // the work list's counter
     // Each thread builds its record in shared memory; the warp then writes
     // the records out with coalesced 16-byte stores.  Only triangles that
@@ -708,24 +709,36 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
     __shared__ __align__(16) uint4 sbuf[RF_SETUP_THREADS][RF_PRIM_CORE_BYTES / 16];
     const uint32_t lane = threadIdx.x & 31, wbase = threadIdx.x & ~31u;
     const uint32_t stride = gridDim.x * blockDim.x;
+    // Depth-sorted frames (perm != nullptr): thread gt is the gt-th clipped
+    // triangle in sorted order, perm[gt] its index in clipped order, ptri
+    // the input triangle it came from; the draws' tri_base / ntri count
+    // clipped triangles then, and src_tri_base locates the input ones.
     for (uint32_t base = blockIdx.x * blockDim.x; base < nt_total; base += stride) {
         const uint32_t gt = base + threadIdx.x;
         const bool active = gt < nt_total;
-        const uint32_t cnt = active ? tcnt[gt] : 0u;
+        const uint32_t cnt = active ? (perm ? 1u : tcnt[gt]) : 0u;
         uint32_t job = 0xFFFFFFFFu;
         unsigned long long prims_o = 0;
-        uint32_t di = 0, t = 0, nc = 0, na = 0, zm = 0, slot = RF_NO_POLY, p0 = 0;
+        uint32_t di = 0, t = 0, nc = 0, na = 0, zm = 0, slot = RF_NO_POLY, p0 = 0, fan0 = 0;
         const uint32_t dwarp = warp_upper_index(nd, active ? gt : nt_total - 1,
                                                 [&](uint32_t i) { return draws[i].tri_base; });
         if (cnt) {
             di = dwarp;
             job = draws[di].job;
-            t = gt - draws[di].tri_base;
             nc = 1 + nattr_of(draws[di].shader);
             na = nc - 1;
             zm = zdiv_mask_of(draws[di].shader);
-            slot = tpoly[gt];
-            p0 = toff[gt];
+            if (perm) {
+                const uint32_t pc = perm[gt], tin = ptri[pc];
+                t = tin - draws[di].src_tri_base;
+                slot = tpoly[tin];
+                fan0 = pc - toff[tin];
+                p0 = gt;
+            } else {
+                t = gt - draws[di].tri_base;
+                slot = tpoly[gt];
+                p0 = toff[gt];
+            }
         }
         const uint32_t maxc = __reduce_max_sync(0xFFFFFFFFu, cnt);
         uint32_t words = 0;  // row-record words of this input triangle so far
@@ -745,7 +758,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const float *src = d.verts + (size_t)li * d.stride + d.pos_dim;
                         for (uint32_t a = 0; a < na; ++a) at[k][a] = src[a];
                     } else {
-                        const PolyVert &v = pool[(size_t)slot * RF_POLY_STORE + (k == 0 ? 0 : c + k)];
+                        const PolyVert &v = pool[(size_t)slot * RF_POLY_STORE + (k == 0 ? 0 : fan0 + c + k)];
 #pragma unroll
                         for (int q = 0; q < 4; ++q) pos[k][q] = v.pos[q];
                         for (uint32_t a = 0; a < na; ++a) at[k][a] = v.a[a];
@@ -1350,7 +1363,8 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
                          RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
-                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s) {
+                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
+                         const uint32_t *perm, const uint32_t *ptri) {
     cudaError_t e;
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
@@ -1358,7 +1372,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
                                                 prims, tri_words, rprims, live,
                                                 counters + RF_CNT_LIVE, counters + RF_CNT_ITEMS,
-                                                stats);
+                                                stats, perm, ptri);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // Row-record offsets of the input triangles (64-bit: the total may not fit 32).
@@ -1439,6 +1453,18 @@ __global__ void __launch_bounds__(256) k_stats_fold(const StatsDev *__restrict__
             t[f] += sum;
         }
     }
+}
+
+// The GPU's global nanosecond timer at this point of the stream.
+__global__ void k_stamp(unsigned long long *dst) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *dst = t;
+}
+
+cudaError_t launch_stamp(unsigned long long *dst, cudaStream_t s) {
+    k_stamp<<<1, 1, 0, s>>>(dst);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_stats_fold(const StatsDev *js, uint32_t n, StatsDev *total, cudaStream_t s) {

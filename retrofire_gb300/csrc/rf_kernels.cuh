@@ -80,7 +80,8 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
                          RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
-                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s);
+                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
+                         const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr);
 // The rasteriser's work list from the tile masks and the marks total
 // (slots: the warps the rasteriser keeps resident, about).  items (room
 // for (RF_SPLIT_K + 1) * ntiles): items[ntiles .. ntiles + extra) first --
@@ -123,6 +124,30 @@ cudaError_t launch_cull(DrawDev *draws, uint32_t nd, StatsDev *stats, int nsm, c
 cudaError_t launch_lines(const DrawDev *draws, const JobDev *jobs, uint32_t nl, const float4 *cpos,
                          const uint8_t *coc, LineRec *recs, uint32_t *mask, uint32_t ntiles,
                          uint32_t *queue, StatsDev *stats, int nsm, cudaStream_t s);
+// Depth sort (render.rs:180-182, 209-219; rf_sort.cu).  launch_dsort: the
+// key of every clipped triangle -- its draw, then Render::depth (the mean
+// clip-space z, prim.rs:21-23) in f32::total_cmp order, ascending or
+// descending per its job's depth_sort (0 for jobs without) -- sorted stably,
+// so perm[r] is the clipped-order index of the r-th triangle; ptri[p] is the
+// input triangle of clipped triangle p.  np = the frame's clipped
+// triangles (host-known); scan_scratch holds
+// scan_scratch_words(dsort_scan_items(np)) words.
+size_t dsort_scratch_bytes(uint32_t np);
+uint32_t dsort_scan_items(uint32_t np);
+cudaError_t launch_dsort(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
+                         uint32_t np, const float4 *cpos, const uint32_t *tcnt, const uint32_t *toff,
+                         const uint32_t *tpoly, const PolyVert *pool, const uint32_t *counters,
+                         uint32_t *perm, uint32_t *ptri, void *scratch, uint32_t *scan_scratch,
+                         cudaStream_t s);
+// Per-draw clipped-triangle counts only (nout[d]), before np is known.
+cudaError_t launch_draw_counts(const DrawDev *draws, uint32_t nd, uint32_t nt, const uint32_t *toff,
+                               const uint32_t *counters, uint32_t *nout, cudaStream_t s);
+// toff[i] = i, tcnt[i] = 1 for i < n: the raster's view of a sorted frame,
+// where every clipped triangle is one unit of the tile masks.
+cudaError_t launch_iota(uint32_t *toff, uint32_t *tcnt, uint32_t n, cudaStream_t s);
+// Writes the GPU's global timer (ns) into *dst when the stream reaches it
+// (dst: device memory or page-locked host memory).
+cudaError_t launch_stamp(unsigned long long *dst, cudaStream_t s);
 // Adds the n per-job stats slots js[0..n) into *total (one block).
 cudaError_t launch_stats_fold(const StatsDev *js, uint32_t n, StatsDev *total, cudaStream_t s);
 }  // namespace rfk

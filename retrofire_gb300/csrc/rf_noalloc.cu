@@ -2,18 +2,21 @@
 // device memory.
 //
 // Who needs it: callers that may not call cudaMalloc at render time — a
-// frame loop running under a fixed, pre-reserved device-memory budget, a
-// plugin living inside a host application that owns every allocation, or
-// code that records its work into a CUDA graph and must not allocate while
-// doing so.  They own their input and output buffers; the library supplies
-// the scratch space from a fixed area compiled into it.
+// frame loop running under a fixed, pre-reserved device-memory budget, or a
+// plugin living inside a host application that owns every allocation and
+// hands the plugin only the buffers it is to fill.  They own their input and
+// output buffers; the library supplies the scratch space from a fixed area
+// compiled into it.
 //
 // The scratch is one file-scope __device__ array of RF_NOALLOC_SCRATCH_BYTES
 // (8 MiB).  Every GPU that loads the library keeps that area until the
 // process exits.  Host code only sees a host-side stand-in for the array's
 // name, so the device address is looked up with cudaGetSymbolAddress, once
 // per device, with that device current, on the first call made on it.  That
-// first call should therefore happen before any stream capture begins.
+// first call should therefore happen before any stream capture begins.  The
+// address is kept for the life of the process: after cudaDeviceReset on a
+// device it is stale, so the call must not be used on a device that was
+// reset since its first call.
 //
 // All calls share the one area and each call overwrites what the previous
 // one left there; the parts that must start at zero are cleared by every
@@ -99,6 +102,16 @@ uint32_t pack(uint32_t c, int32_t fmt) {
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_rf_noalloc_scratch[RF_NOALLOC_SCRATCH_BYTES];
 
+// The one draw's and the one job's descriptors, passed by value as kernel
+// parameters and written into the scratch area on the stream (no host
+// buffer has to outlive the call).
+__global__ void k_na_put(DrawDev d, JobDev J, DrawDev *dd, JobDev *jd) {
+    if (threadIdx.x == 0) {
+        *dd = d;
+        *jd = J;
+    }
+}
+
 // On failure the runtime's last-error state is cleared too, so the
 // launches of a later call do not report this error as theirs.
 #define NA_CK(call)                              \
@@ -125,9 +138,13 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     if (nattr != nattr_of(shader)) return RF_ERR_BAD_ARG;
     if (pixfmt < RF_ARGB8888 || pixfmt > RF_BGRA8888) return RF_ERR_BAD_ARG;
     if (flags->depth_test < RF_DEPTH_NONE || flags->depth_test > RF_DEPTH_GREATER ||
-        flags->face_cull < RF_CULL_NONE || flags->face_cull > RF_CULL_FRONT)
+        flags->face_cull < RF_CULL_NONE || flags->face_cull > RF_CULL_FRONT ||
+        flags->depth_sort != RF_SORT_NONE)  // depth sorting needs scratch this area lacks
         return RF_ERR_BAD_ARG;
     if ((ntri && (!idx || !verts)) || (nverts && !verts)) return RF_ERR_BAD_ARG;
+    // Triangles without vertices: every index would be out of range (the
+    // reference panics on `vs[i]`, prim.rs:17-19).
+    if (ntri && !nverts) return RF_ERR_BAD_ARG;
     if (ntri > RF_NOALLOC_MAX_TRIS || nverts > RF_NOALLOC_MAX_VERTS || w > RF_NOALLOC_MAX_W ||
         h > RF_NOALLOC_MAX_H)
         return RF_ERR_OVER_BUDGET;  // beyond the fixed scratch area
@@ -230,13 +247,13 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     // ---- zero what the kernels accumulate into, then the pass itself
     NA_CK(cudaMemsetAsync(sd, 0, sizeof(StatsDev), s));
     NA_CK(cudaMemsetAsync(cnt, 0, RF_CNT_N * 4, s));
-    if (ntri == 0 || nverts == 0) {
+    if (ntri == 0) {
         if (J.clear_flags)
             NA_CK(rfk::launch_fill(color, depth, (size_t)w * h, J.clear_px, J.clear_z,
                                    J.clear_flags, nsm, s));
     } else {
-        NA_CK(cudaMemcpyAsync(dd, &d, sizeof d, cudaMemcpyHostToDevice, s));
-        NA_CK(cudaMemcpyAsync(jd, &J, sizeof J, cudaMemcpyHostToDevice, s));
+        k_na_put<<<1, 32, 0, s>>>(d, J, dd, jd);
+        NA_CK(cudaGetLastError());
         NA_CK(cudaMemsetAsync(mask, 0, (size_t)ntiles * (J.mask_words + J.sum_words) * 4, s));
         NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, cnt, marks, nsm, s));
         NA_CK(rfk::launch_clip(dd, 1, ntri, cpos, coc, tcnt, tpoly, toff, pool, RF_NOALLOC_MAX_TRIS,

@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "rf_device.cuh"
 
 // ---------------------------------------------------------------------------
@@ -762,11 +764,81 @@ struct Pipe {
     static constexpr uint32_t HS = (uint32_t)HA + 1u;  // header slots
     static constexpr uint32_t RS = (uint32_t)RA + 1u;  // row-record slots
 };
+// The header and row-record rings double as the row-major staging buffer
+// of the coalesced tile load and store (32 rows of min(TW, 32) + 1 words),
+// so the region is the larger of the two.
+template <int TW, int KIND>
+__host__ __device__ constexpr uint32_t raster_ring_words() {
+    return Pipe<TW>::HS * (uint32_t)(sizeof(RasterPrim) / 4) +
+           Pipe<TW>::RS * rfr::row_words(rfr::PreNC<KIND>::NC) * RF_TILE_H;
+}
+template <int TW>
+__host__ __device__ constexpr uint32_t raster_stage_words() {
+    return RF_TILE_H * ((TW < 32 ? (uint32_t)TW : 32u) + 1u);
+}
 template <int TW, int KIND>
 __host__ __device__ constexpr uint32_t raster_warp_words() {
-    return 2u * TW * RF_TILE_H + Pipe<TW>::HS * (uint32_t)(sizeof(RasterPrim) / 4) +
-           Pipe<TW>::RS * rfr::row_words(rfr::PreNC<KIND>::NC) * RF_TILE_H + ((uint32_t)TW / RF_SEG) * RF_TILE_H;
+    return 2u * TW * RF_TILE_H +
+           (raster_ring_words<TW, KIND>() > raster_stage_words<TW>() ? raster_ring_words<TW, KIND>()
+                                                                     : raster_stage_words<TW>()) +
+           ((uint32_t)TW / RF_SEG) * RF_TILE_H;
 }
+
+namespace rfr {
+
+// Coalesced transfer between a tile's global rows and its column-major
+// shared-memory copy (word x * 32 + r): 16-byte accesses with the lanes of a
+// row side by side (8 lanes per 128 bytes), through a row-major staging
+// buffer of stride CB + 1 (CB = columns per pass, at most 32) whose odd
+// stride keeps both sides free of bank conflicts.  Only the rows with bit r
+// of `want` set are moved.  Every moved row must hold TW columns inside the
+// target and start 16-byte aligned.
+template <int TW, bool LOAD>
+__device__ __forceinline__ void tile_rows_coalesced(uint32_t *__restrict__ tile, uint32_t *__restrict__ stg,
+                                                    uint32_t *__restrict__ g, uint32_t pitch,
+                                                    uint32_t want, uint32_t lane) {
+    constexpr uint32_t CB = TW < 32 ? TW : 32;   // columns per pass
+    constexpr uint32_t LPR = CB / 4;             // lanes per row
+    constexpr uint32_t RPI = 32 / LPR;           // rows per instruction
+    constexpr uint32_t SS = CB + 1;              // staging stride
+    const uint32_t lr = lane / LPR, lc = (lane % LPR) * 4;
+#pragma unroll 1
+    for (uint32_t x0 = 0; x0 < (uint32_t)TW; x0 += CB) {
+        if constexpr (LOAD) {
+#pragma unroll
+            for (uint32_t r0 = 0; r0 < 32; r0 += RPI) {
+                const uint32_t r = r0 + lr;
+                if ((want >> r) & 1u) {
+                    const uint4 v = *reinterpret_cast<const uint4 *>(g + (size_t)r * pitch + x0 + lc);
+                    uint32_t *d = stg + r * SS + lc;
+                    d[0] = v.x;
+                    d[1] = v.y;
+                    d[2] = v.z;
+                    d[3] = v.w;
+                }
+            }
+            __syncwarp();
+#pragma unroll 4
+            for (uint32_t x = 0; x < CB; ++x) tile[(x0 + x) * RF_TILE_H + lane] = stg[lane * SS + x];
+            __syncwarp();
+        } else {
+#pragma unroll 4
+            for (uint32_t x = 0; x < CB; ++x) stg[lane * SS + x] = tile[(x0 + x) * RF_TILE_H + lane];
+            __syncwarp();
+#pragma unroll
+            for (uint32_t r0 = 0; r0 < 32; r0 += RPI) {
+                const uint32_t r = r0 + lr;
+                if ((want >> r) & 1u) {
+                    const uint32_t *sp = stg + r * SS + lc;
+                    *reinterpret_cast<uint4 *>(g + (size_t)r * pitch + x0 + lc) = make_uint4(sp[0], sp[1], sp[2], sp[3]);
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+}  // namespace rfr
 
 // KIND: shader kind of every draw of the job (or RF_K_ANY); FAST: the
 // default context (depth test Less, colour and depth writes) on a target
@@ -788,7 +860,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
     float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
     RasterPrim *stage = reinterpret_cast<RasterPrim *>(scol + 2 * TW * RF_TILE_H);
     uint32_t *rslots = scol + 2 * TW * RF_TILE_H + Pipe<TW>::HS * (sizeof(RasterPrim) / 4);
-    float *smin = reinterpret_cast<float *>(rslots + Pipe<TW>::RS * RW);
+    uint32_t *stg = scol + 2 * TW * RF_TILE_H;  // tile staging (the rings, when idle)
+    float *smin = reinterpret_cast<float *>(scol + WARP_WORDS - ((uint32_t)TW / RF_SEG) * RF_TILE_H);
     // Queue position q: the heavy tiles and crowded-tile slices first
     // (items[ntiles + q]), then every other tile in index order.
     const uint32_t nfirst = *nitems_dev;
@@ -818,7 +891,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         T.tx0 = txi * TW;
         T.tx1 = min(T.tx0 + (uint32_t)TW, J.w);
         T.tw = TW;
-        T.y = tyi * RF_TILE_H + lane;
+        const uint32_t ty0 = tyi * RF_TILE_H;
+        T.y = ty0 + lane;
         constexpr uint32_t SLICE_H = RF_TILE_H / RF_SPLIT_K;
         T.row_ok = T.y < J.h && (slice == 0 || lane / SLICE_H == slice - 1u);
         T.has_depth = J.depth != nullptr;
@@ -829,27 +903,28 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         T.frags_o = 0;
         const uint32_t ncols = T.tx1 - T.tx0;
         const size_t row_off = (size_t)T.y * J.w + T.tx0;
-        // Lane r moves row r; 16-byte vectors when the row start is aligned.
+        const uint32_t rows_ok = __ballot_sync(0xFFFFFFFFu, T.row_ok);
+        // Coalesced 16-byte row transfers (tile_rows_coalesced) when the
+        // tile's rows hold its full width and start 16-byte aligned.
         const bool vec = ((J.w | T.tx0) & 3u) == 0u && ncols == (uint32_t)TW &&
                          (((uintptr_t)J.color | (uintptr_t)J.depth) & 15u) == 0u;
+        uint32_t *gcol = J.color + (size_t)ty0 * J.w + T.tx0;
+        uint32_t *gdep = reinterpret_cast<uint32_t *>(J.depth) + (size_t)ty0 * J.w + T.tx0;
         bool loaded = false;
         auto load_tile = [&]() {
             const bool cc = J.clear_flags & 1u, cd = (J.clear_flags & 2u) != 0u;
-            if (vec && T.row_ok && !(cc && cd)) {
-                for (uint32_t x = 0; x < (uint32_t)TW; x += 4) {
-                    uint4 c4 = cc ? make_uint4(J.clear_px, J.clear_px, J.clear_px, J.clear_px)
-                                  : *reinterpret_cast<const uint4 *>(J.color + row_off + x);
-                    scol[(x + 0) * RF_TILE_H + lane] = c4.x;
-                    scol[(x + 1) * RF_TILE_H + lane] = c4.y;
-                    scol[(x + 2) * RF_TILE_H + lane] = c4.z;
-                    scol[(x + 3) * RF_TILE_H + lane] = c4.w;
-                    if (T.has_depth) {
-                        float4 d4 = cd ? make_float4(J.clear_z, J.clear_z, J.clear_z, J.clear_z)
-                                       : *reinterpret_cast<const float4 *>(J.depth + row_off + x);
-                        sdep[(x + 0) * RF_TILE_H + lane] = d4.x;
-                        sdep[(x + 1) * RF_TILE_H + lane] = d4.y;
-                        sdep[(x + 2) * RF_TILE_H + lane] = d4.z;
-                        sdep[(x + 3) * RF_TILE_H + lane] = d4.w;
+            if (vec) {
+                if (cc) {
+                    for (uint32_t x = 0; x < (uint32_t)TW; ++x) scol[x * RF_TILE_H + lane] = J.clear_px;
+                } else {
+                    tile_rows_coalesced<TW, true>(scol, stg, gcol, J.w, rows_ok, lane);
+                }
+                if (T.has_depth) {
+                    if (cd) {
+                        for (uint32_t x = 0; x < (uint32_t)TW; ++x) sdep[x * RF_TILE_H + lane] = J.clear_z;
+                    } else {
+                        tile_rows_coalesced<TW, true>(reinterpret_cast<uint32_t *>(sdep), stg, gdep, J.w,
+                                                      rows_ok, lane);
                     }
                 }
             } else {
@@ -938,18 +1013,12 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
             load_tile();
             loaded = true;
         }
-        if (loaded && T.row_ok) {
+        if (loaded) {
             if (vec) {
-                for (uint32_t x = 0; x < (uint32_t)TW; x += 4) {
-                    *reinterpret_cast<uint4 *>(J.color + row_off + x) =
-                        make_uint4(scol[(x + 0) * RF_TILE_H + lane], scol[(x + 1) * RF_TILE_H + lane],
-                                   scol[(x + 2) * RF_TILE_H + lane], scol[(x + 3) * RF_TILE_H + lane]);
-                    if (T.has_depth)
-                        *reinterpret_cast<float4 *>(J.depth + row_off + x) =
-                            make_float4(sdep[(x + 0) * RF_TILE_H + lane], sdep[(x + 1) * RF_TILE_H + lane],
-                                        sdep[(x + 2) * RF_TILE_H + lane], sdep[(x + 3) * RF_TILE_H + lane]);
-                }
-            } else {
+                tile_rows_coalesced<TW, false>(scol, stg, gcol, J.w, rows_ok, lane);
+                if (T.has_depth)
+                    tile_rows_coalesced<TW, false>(reinterpret_cast<uint32_t *>(sdep), stg, gdep, J.w, rows_ok, lane);
+            } else if (T.row_ok) {
                 for (uint32_t x = 0; x < ncols; ++x) {
                     const uint32_t i = x * RF_TILE_H + lane;
                     J.color[row_off + x] = scol[i];
@@ -965,6 +1034,30 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
 
 namespace rfk {
 
+// The opt-in to more than 48 KB of dynamic shared memory is a property of
+// each kernel on each device: set once per (kernel, device) -- the flags
+// live in the instantiation for that kernel (Tag), since every k_raster
+// variant has the same function type -- under a lock so host threads
+// driving contexts on several devices may launch concurrently, and with
+// its status returned.
+template <class Tag, class K>
+static cudaError_t opt_in_smem(K kernel, int bytes) {
+    constexpr int MAX_DEV = 64;
+    static std::mutex mu;
+    static bool done[MAX_DEV] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEV) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!done[dev]) {
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        done[dev] = true;
+    }
+    return cudaSuccess;
+}
+
 template <int TW, int KIND, bool FAST>
 static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDev *draws,
                                    const PrimRec *prims, const RasterPrim *rprims,
@@ -978,11 +1071,9 @@ static cudaError_t launch_raster_k(const JobDev *jobs, uint32_t nj, const DrawDe
     constexpr size_t per_warp = (size_t)raster_warp_words<TW, KIND>() * 4;
     if ((size_t)warps * per_warp > SMEM_MAX) warps = (uint32_t)(SMEM_MAX / per_warp);
     const size_t smem = (size_t)warps * per_warp;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_raster<TW, KIND, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_MAX);
-        attr_set = true;
-    }
+    struct Tag {};  // one per (TW, KIND, FAST)
+    cudaError_t e = opt_in_smem<Tag>(k_raster<TW, KIND, FAST>, (int)SMEM_MAX);
+    if (e != cudaSuccess) return e;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster<TW, KIND, FAST>, warps * 32, smem);
     if (per_sm < 1) per_sm = 1;

@@ -131,17 +131,15 @@ def fill_stress(ntri=100_000, w=1920, h=1080, seed=2, cross_frac=0.05, amin=1.0,
     return dict(verts=verts, faces=faces, vp=mat.viewport(0, 0, w, h), w=w, h=h, pos_dim=4)
 
 
-def _look_at(eye, target):
-    eye = np.asarray(eye, np.float64)
-    f = np.asarray(target, np.float64) - eye
-    f /= np.linalg.norm(f)
-    rgt = np.cross([0.0, 1.0, 0.0], f)
-    rgt /= np.linalg.norm(rgt)
-    up = np.cross(f, rgt)
-    m = np.eye(4)
-    m[0, :3], m[1, :3], m[2, :3] = rgt, up, f
-    m[:3, 3] = -m[:3, :3] @ eye
-    return m.astype(f32)
+def first_person_camera(eye, target, w, h, focal_ratio_of_aspect, near, far):
+    """Camera::new((w, h)) with a FirstPerson transform at `eye` looking at
+    `target`, the viewport flipped to y-down rows as demos/src/bin/crates.rs
+    sets it ((0..w, h..0)), and a perspective projection
+    (render/cam.rs:146-224).  Returns the Camera."""
+    fp = mat.FirstPerson(eye)
+    fp.look_at(target)
+    return (mat.Camera((w, h)).with_transform(fp).viewport((0, w), (h, 0))
+            .perspective(focal_ratio_of_aspect, near, far))
 
 
 def instanced_cubes(ninst=10_000, w=1920, h=1080, seed=3, tex_size=1024):
@@ -151,10 +149,11 @@ def instanced_cubes(ninst=10_000, w=1920, h=1080, seed=3, tex_size=1024):
     tx = rng.uniform(-100.0, 100.0, size=ninst)
     tz = rng.uniform(-100.0, 100.0, size=ninst)
     yaw = rng.uniform(0.0, 2 * np.pi, size=ninst)
-    view = _look_at([0.0, 2.0, -110.0], [0.0, 0.0, 0.0])
-    aspect = f32(w) / f32(h)
-    proj = mat.perspective(mat.focal_ratio_diagonal(np.pi / 2.0, aspect), aspect, 0.1, 1000.0)
-    vp_proj = mat.then(view, proj)
+    # demos/src/bin/crates.rs:51-54: FirstPerson camera, Fov::Diagonal(90 deg),
+    # near..far 0.1..1000; here at (0, 2, -110) looking at the origin.
+    cam = first_person_camera([0.0, 2.0, -110.0], [0.0, 0.0, 0.0], w, h,
+                              lambda a: mat.focal_ratio_diagonal(np.pi / 2.0, a), 0.1, 1000.0)
+    vp_proj = cam.world_to_project()
     sc = np.zeros((ninst, 4, 4), f32)
     sc[:, 0, 0] = sc[:, 1, 1] = sc[:, 2, 2] = scale
     sc[:, 3, 3] = 1.0
@@ -168,7 +167,7 @@ def instanced_cubes(ninst=10_000, w=1920, h=1080, seed=3, tex_size=1024):
     mvps = mat.then(model, vp_proj)
     verts, faces = cube_mesh(1.0, "col_uv")
     return dict(verts=verts, faces=faces, tex=noise_texture(tex_size, seed + 100), mvps=mvps,
-                vp=mat.viewport(0, h, w, 0), w=w, h=h)
+                vp=cam.viewport_m, w=w, h=h)
 
 
 def batch_scenes(nscenes=256, seed=4, min_tris=12, max_tris=200_000, wmin=64, wmax=1920,
@@ -246,9 +245,9 @@ def orbit_camera(seed, w, h, dist=(2.4, 3.6), pitch=(0.35, 1.0)):
     pt = rng.uniform(*pitch)
     d = rng.uniform(*dist)
     eye = [d * np.cos(pt) * np.sin(yaw), d * np.sin(pt), -d * np.cos(pt) * np.cos(yaw)]
-    aspect = f32(w) / f32(h)
-    proj = mat.perspective(mat.focal_ratio_horizontal(np.pi / 3.0), aspect, 0.1, 100.0)
-    return mat.then(_look_at(eye, [0.0, 0.0, 0.0]), proj)
+    cam = first_person_camera(eye, [0.0, 0.0, 0.0], w, h,
+                              lambda a: mat.focal_ratio_horizontal(np.pi / 3.0), 0.1, 100.0)
+    return cam.world_to_project()
 
 
 def serving_requests(n, rate, seed=5, meshes=SERVING_MESHES, resolutions=SERVING_RESOLUTIONS):

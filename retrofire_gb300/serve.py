@@ -43,7 +43,8 @@ class MeshSet:
         self.texture.close()
 
 
-def run_load(server, meshset, requests, realtime=True, pixfmt=ARGB8888, depth=True):
+def run_load(server, meshset, requests, realtime=True, pixfmt=ARGB8888, depth=True,
+             read_depth=None):
     """Submits `requests` (scenes.serving_requests) to `server` at their
     arrival offsets (or all at once when realtime is False) from one thread
     while this thread collects the results.  Returns (results, wall_s) with
@@ -60,7 +61,8 @@ def run_load(server, meshset, requests, realtime=True, pixfmt=ARGB8888, depth=Tr
                     if dt > 0:
                         time.sleep(dt)
                 tickets[i] = server.submit(meshset.draws(r), r["vp"], r["w"], r["h"],
-                                           ctx=Context(), pixfmt=pixfmt, depth=depth)
+                                           ctx=Context(), pixfmt=pixfmt, depth=depth,
+                                           read_depth=read_depth)
         except Exception as e:  # surfaced to the caller below
             errors.append(e)
 
@@ -78,6 +80,51 @@ def run_load(server, meshset, requests, realtime=True, pixfmt=ARGB8888, depth=Tr
     if errors:
         raise errors[0]
     return out, time.perf_counter() - t0
+
+
+def run_per_frame(device, meshset, requests, realtime=True, depth=True, read_depth=False):
+    """The plain per-frame drop-in serving the same stream: one thread takes
+    the requests in arrival order and, for each, clears a target of its
+    size (with a depth buffer when `depth`), renders it with one
+    rf_render_draws and reads the image back (colour, and depth when
+    read_depth) before taking the next.  Latency runs from the request's
+    arrival to its image being in host memory.  Returns (results, wall_s)
+    shaped like run_load's (batch_size 1)."""
+    from . import Framebuf, render_draws
+    targets = {}
+    out = []
+    ctx = Context()
+    t0 = time.perf_counter()
+    for r in requests:
+        arrival = t0 + r["t"] if realtime else time.perf_counter()
+        if realtime:
+            dt = arrival - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+        start = time.perf_counter()
+        key = (r["w"], r["h"])
+        if key not in targets:
+            targets[key] = Framebuf(r["w"], r["h"], ARGB8888, depth, device=device)
+        tg = targets[key]
+        tg.clear(ctx.color_clear, ctx.depth_clear)
+        st = render_draws(meshset.draws(r), r["vp"], tg, ctx, sync_stats=True)
+        col, dep = tg.read() if (depth and read_depth) else (_read_color(tg), None)
+        done = time.perf_counter()
+        out.append((col, dep, {"status": 0, "batch_size": 1,
+                               "queue_ms": 1e3 * max(0.0, start - arrival),
+                               "render_ms": 1e3 * (done - start),
+                               "total_ms": 1e3 * (done - arrival), "stats": st}))
+    wall = time.perf_counter() - t0
+    for tg in targets.values():
+        tg.close()
+    return out, wall
+
+
+def _read_color(tg):
+    from . import _check, _u32p, lib
+    color = np.empty((tg.h, tg.w), np.uint32)
+    _check(lib().rf_target_read(tg.dev.ptr, tg.handle, _u32p(color), None), "rf_target_read")
+    return color
 
 
 def latency_summary(results):

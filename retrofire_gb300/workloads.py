@@ -10,6 +10,7 @@ share a vertex array share one device mesh.
   batch   256 uneven independent scenes (scenes.batch_scenes)
   serve   the first requests of the serving stream as scenes
 """
+import ctypes as C
 import functools
 import time
 
@@ -181,6 +182,39 @@ def e2e(objs, dev, steps, warmup, objs2=None):
                     "copy streams, wall clock to the final sync" % len(sets),
             "latency_ms": {"p50": ms[len(ms) // 2], "p99": ms[min(len(ms) - 1, int(0.99 * len(ms)))],
                            "note": "one synchronous step: upload, render, read back"}}
+
+
+def render_per_frame(scenes_, device, sync_stats=False):
+    """The plain per-frame drop-in over a batch's scenes: one
+    rf_render_draws (one frame of render() calls into one target) per
+    scene, in order, on the device's stream.  Returns each scene's Stats
+    when sync_stats is set."""
+    from . import CStats, Stats, _check, _fp, lib
+    L = lib()
+    out = []
+    for sc in scenes_:
+        arr = sc._draw_array()
+        fl = sc.ctx.flags()
+        cs = CStats() if sync_stats else None
+        _check(L.rf_render_draws(device.ptr, arr, len(sc.draws), _fp(sc.to_screen),
+                                 sc.target.handle, C.byref(fl), C.byref(cs) if cs else None),
+               "rf_render_draws")
+        if sync_stats:
+            out.append(Stats.from_c(cs))
+    return out if sync_stats else None
+
+
+def target_digests(targets):
+    """blake2b of every target's colour and depth bytes (read back)."""
+    import hashlib
+    out = []
+    for tg in targets:
+        c, d = tg.read()
+        h = hashlib.blake2b(c.tobytes(), digest_size=16)
+        if d is not None:
+            h.update(d.tobytes())
+        out.append(h.hexdigest())
+    return out
 
 
 def close(objs):

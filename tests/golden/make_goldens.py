@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference tree.
 
-Run in a container where the retrofire reference is mounted (default
-/root/reference, or pass its path).  It copies the reference's own golden
+Run where the retrofire reference tree is available: pass its path as the
+first argument, or set RETROFIRE_REF (the default is where this build's
+container mounts it, /root/reference).  It copies the reference's own golden
 images and the expected values written in its unit tests (read as text),
 so that the tests can pin the oracle without the reference present:
 
@@ -18,7 +19,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("RETROFIRE_REF", "/root/reference")
 
 
 def parse_ppm(data):

@@ -19,7 +19,7 @@ class DrawSpec:
 
 def ctx_dict(ctx):
     return dict(depth_test=ctx.depth_test, color_write=ctx.color_write,
-                depth_write=ctx.depth_write, face_cull=ctx.face_cull)
+                depth_write=ctx.depth_write, face_cull=ctx.face_cull, depth_sort=ctx.depth_sort)
 
 
 def gpu_render(draws, vp, w, h, ctx=None, pixfmt=rf.ARGB8888, depth=True, clear=True,

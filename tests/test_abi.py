@@ -42,11 +42,13 @@ def test_python_bindings_cover_header(libpath):
 
 
 def test_rust_binding_covers_header():
-    """The -sys binding in INTEGRATION.md declares every entry point."""
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    bound = set(re.findall(r"\bfn (rf_[a-z_0-9]+)\s*\(", doc))
-    missing = [s for s in declared_symbols() if s not in bound]
-    assert not missing, missing
+    """The Rust -sys crate (retrofire_gb300/rust/rf-gpu-sys) declares every
+    entry point of the header, and no other."""
+    src = open(os.path.join(ROOT, "retrofire_gb300", "rust", "rf-gpu-sys", "src", "lib.rs")).read()
+    bound = set(re.findall(r"\bpub fn (rf_[a-z_0-9]+)\s*\(", src))
+    declared = set(declared_symbols())
+    assert declared <= bound, sorted(declared - bound)
+    assert bound <= declared, sorted(bound - declared)
 
 
 def test_status_strings(libpath):

@@ -1,13 +1,16 @@
 """The serving loop (rf_server): continuous batching must not change any
 request's result.  Every request's image and stats equal the oracle's
 render() of its scene on a cleared target and the same request served
-alone; admission refuses what the budget cannot hold; a bad request fails
-alone."""
+alone; a request submitted while another batch is on the device overlaps
+it there; admission keeps the charges in flight within the budget and
+refuses what the budget cannot hold; a bad request fails alone."""
+import time
+
 import numpy as np
 import pytest
 
 import retrofire_gb300 as rf
-from retrofire_gb300 import scenes, serve
+from retrofire_gb300 import mat, scenes, serve
 from rfhelp import DrawSpec, assert_parity, oracle_render
 
 pytestmark = pytest.mark.gpu
@@ -55,18 +58,30 @@ def test_mix_equals_alone_and_oracle():
         dev.close()
 
 
+def charge(w, h, ntri, nverts, depth=True):
+    """The admission charge of one request (include/rfgpu.h): target,
+    scratch per triangle and vertex, tile masks at 8x32-pixel tiles."""
+    tiles = ((w + 7) // 8) * ((h + 31) // 32)
+    mw = (ntri + 31) // 32
+    return (w * h * 4 * (2 if depth else 1) + ntri * 5632 + nverts * 24
+            + tiles * (mw + (mw + 31) // 32) * 4)
+
+
 def test_budget_bounds_batches():
-    """A budget that holds about two requests splits the stream into
-    batches of at most that many; results are unchanged."""
+    """A budget that holds two requests: no batch is larger, the charges in
+    flight over all pipelines never exceed it, and results are unchanged."""
     dev = rf.Device()
     ms = serve.MeshSet(dev, SMALL[:2])
     reqs = scenes.serving_requests(12, 1000.0, seed=13, meshes=SMALL[:2],
                                    resolutions=((320, 240, 1.0),))
-    one = 320 * 240 * 8 + 128 * rf_bytes_per_tri() + 81 * 24
-    srv = rf.Server(dev, hbm_budget_bytes=2 * one + 1000)
+    one = max(charge(320, 240, len(e[4]), len(e[3])) for e in ms.entries)
+    budget = 2 * one + 1000
+    srv = rf.Server(dev, hbm_budget_bytes=budget, inflight=3)
     try:
         res, _ = serve.run_load(srv, ms, reqs, realtime=False)
         assert max(r[2]["batch_size"] for r in res) <= 2
+        m = srv.memory()
+        assert 0 < m["peak_charged"] <= budget and m["charged"] == 0
         for i, (r, (c, d, st)) in enumerate(zip(reqs, res)):
             assert_parity((c, d, st["stats"]), oracle_of(ms, r), what="request %d" % i)
     finally:
@@ -75,8 +90,56 @@ def test_budget_bounds_batches():
         dev.close()
 
 
-def rf_bytes_per_tri():
-    return 5632
+def test_request_overlaps_batch_in_flight():
+    """A request submitted while another pipeline's batch is on the GPU is
+    admitted at once and its GPU work overlaps that batch's (the global-timer
+    stamps at each batch's start and end intersect); its image equals the
+    same request served alone and the oracle, and so does the big one's."""
+    dev = rf.Device()
+    ms = serve.MeshSet(dev)  # grid500k is entry 4
+    big = dict(mesh=4, w=1920, h=1080, mvp=scenes.orbit_camera(77, 1920, 1080),
+               vp=mat.viewport(0, 1080, 1920, 0))
+    small = dict(mesh=0, w=320, h=240, mvp=scenes.orbit_camera(78, 320, 240),
+                 vp=mat.viewport(0, 240, 320, 0))
+    srv = rf.Server(dev, max_batch=1, inflight=2)
+    try:
+        def sub(r):
+            return srv.submit(ms.draws(r), r["vp"], r["w"], r["h"])
+        # Both pipelines see both shapes first (arenas sized, tiling settled).
+        for _ in range(6):
+            ts = [sub(big), sub(small)]
+            for t in ts:
+                srv.wait(t)
+        alone = srv.wait(sub(small))
+        overlapped = False
+        for _ in range(5):
+            tb = sub(big)
+            t0 = time.perf_counter()
+            while srv.counts()["queued"] and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.0001)
+            tsm = sub(small)
+            cs, ds, rs = srv.wait(tsm)
+            cb, db, rb = srv.wait(tb)
+            assert rs["status"] == 0 and rb["status"] == 0
+            assert rs["batch_size"] == 1 and rb["batch_size"] == 1
+            assert np.array_equal(cs, alone[0])
+            assert np.array_equal(ds.view(np.uint32), alone[1].view(np.uint32))
+            assert rs["stats"].as_dict() == alone[2]["stats"].as_dict()
+            if (rs["pipeline"] != rb["pipeline"]
+                    and max(rs["gpu_start_ns"], rb["gpu_start_ns"])
+                    < min(rs["gpu_end_ns"], rb["gpu_end_ns"])):
+                overlapped = True
+                break
+        assert overlapped, "no overlap: small %r big %r" % (
+            (rs["pipeline"], rs["gpu_start_ns"], rs["gpu_end_ns"]),
+            (rb["pipeline"], rb["gpu_start_ns"], rb["gpu_end_ns"]))
+        assert srv.memory()["peak_inflight"] >= 2
+        assert_parity((cs, ds, rs["stats"]), oracle_of(ms, small), what="small request")
+        assert_parity((cb, db, rb["stats"]), oracle_of(ms, big), what="big request")
+    finally:
+        srv.close()
+        ms.close()
+        dev.close()
 
 
 def test_over_budget_and_bad_request():

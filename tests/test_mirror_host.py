@@ -19,9 +19,13 @@ def test_context_defaults_are_context_default():
     assert (g.depth_test, g.color_write, g.depth_write, g.face_cull) == (rf.DEPTH_GREATER, 0, 0, rf.CULL_NONE)
 
 
-def test_depth_sort_is_refused():
-    with pytest.raises(NotImplementedError):
-        rf.Context(depth_sort="front_to_back")
+def test_depth_sort_flag():
+    """Context::depth_sort defaults to None (ctx.rs:117-126) and travels in
+    rf_context_flags."""
+    assert rf.Context().flags().depth_sort == rf.SORT_NONE
+    assert rf.Context(depth_sort=None).flags().depth_sort == rf.SORT_NONE
+    assert rf.Context(depth_sort=rf.SORT_BACK_TO_FRONT).flags().depth_sort == 2
+    assert rf.Context(depth_sort=rf.SORT_FRONT_TO_BACK).flags().depth_sort == 1
 
 
 def test_stats_accumulate():

@@ -195,3 +195,27 @@ def test_rand_kats():
     g = Xorshift64()
     assert [float(g.uniform(-1.0, 1.0)) for _ in range(3)] == [
         float(np.float32(0.19692874)), float(np.float32(-0.7686298)), float(np.float32(0.91969657))]
+
+
+def test_oracle_depth_sort_orders_by_mean_clip_z():
+    """render.rs:209-219 in the oracle: one render() call of three
+    triangles covering the same pixels, at clip-space z 0.2, 0.5, 0.8 and
+    w 1, 2, 3 (x, y scaled by w), submitted in that order, no depth test:
+    the depth buffer keeps 1/w of the triangle drawn last.  Unsorted and
+    front to back that is the far one (w 3); back to front the near one."""
+    import numpy as np
+    from oracle import oracle as O
+    from retrofire_gb300 import mat
+    verts = []
+    for z, w in ((0.2, 1.0), (0.5, 2.0), (0.8, 3.0)):
+        verts += [[-0.8 * w, -0.8 * w, z, w], [0.8 * w, -0.8 * w, z, w], [0.0, 0.8 * w, z, w]]
+    verts = np.array(verts, np.float32)
+    faces = np.arange(9, dtype=np.uint32).reshape(3, 3)
+    vp = mat.viewport(0, 64, 64, 0)
+    for sort, last_w in ((0, 3.0), (1, 3.0), (2, 1.0)):
+        col = np.zeros((64, 64), np.uint32)
+        dep = np.zeros((64, 64), np.float32)
+        d = O.make_draw(verts, faces, 0, pos_dim=4, flat_rgba=0xFFFFFFFF)
+        st = O.render([d], vp, col, dep, dict(depth_test=0, face_cull=0, depth_sort=sort))
+        assert st.prims_o == 3
+        assert dep[32, 32] == np.float32(1.0) / np.float32(last_w), (sort, dep[32, 32])

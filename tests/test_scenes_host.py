@@ -86,3 +86,26 @@ def test_batch_recipe():
     assert 0.35 < np.mean(np.array(tris) < np.sqrt(12 * 200_000)) < 0.65
     again = scenes.batch_scenes(nscenes=4)
     assert [s["w"] for s in again] == [s["w"] for s in b[:4]]
+
+
+def test_first_person_camera():
+    """FirstPerson (render/cam.rs:403-418) restated: the camera position maps
+    to the view-space origin, the looked-at point onto the +z axis at its
+    distance, world up stays up; Camera composes view then projection."""
+    from retrofire_gb300 import mat
+    for eye, tgt in (([0.0, 2.0, -110.0], [0.0, 0.0, 0.0]), ([3.0, 1.5, 2.0], [0.5, 0.0, -0.2])):
+        fp = mat.FirstPerson(eye)
+        fp.look_at(tgt)
+        v = fp.world_to_view()
+        o = mat.apply_point(v, eye)
+        assert np.allclose(o[:3], 0.0, atol=1e-4)
+        t = mat.apply_point(v, tgt)
+        dist = np.linalg.norm(np.subtract(tgt, eye))
+        assert np.allclose(t[:2], 0.0, atol=1e-4 * dist) and abs(t[2] - dist) < 1e-4 * dist
+        up = v[:3, :3] @ np.array([0.0, 1.0, 0.0], np.float32)
+        assert up[1] > 0.9
+    cam = (mat.Camera((640, 480)).with_transform(fp).viewport((0, 640), (480, 0))
+           .perspective(lambda a: mat.focal_ratio_horizontal(np.pi / 3.0), 0.1, 100.0))
+    assert cam.dims == (640, 480)
+    assert np.array_equal(cam.viewport_m, mat.viewport(0, 480, 640, 0))
+    assert np.array_equal(cam.world_to_project(), mat.then(fp.world_to_view(), cam.project))

@@ -74,7 +74,7 @@ class _FakeServer:
     def __init__(self, fail_at=None):
         self.sub, self.fail_at, self.n = {}, fail_at, 0
 
-    def submit(self, draws, vp, w, h, ctx=None, pixfmt=0, depth=True):
+    def submit(self, draws, vp, w, h, ctx=None, pixfmt=0, depth=True, read_depth=None):
         if self.n == self.fail_at:
             raise rf.RfError(2, "rf_server_submit")
         self.n += 1

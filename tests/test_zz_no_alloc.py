@@ -1,19 +1,20 @@
 """rf_render_noalloc: rendering without any device allocation.
 
 Some callers of this library may not allocate device memory while they
-render: a frame loop held to a fixed, pre-reserved memory budget, a plugin
-inside a host application that owns every allocation, or code that records
-its work into a CUDA graph.  rf_render_noalloc serves them: the caller
-passes its own device buffers for the mesh, texture and target, and the
-library's temporaries live in a fixed scratch area compiled into it.
+render: a frame loop held to a fixed, pre-reserved memory budget, or a
+plugin inside a host application that owns every allocation and only lends
+the plugin the buffers it reads and fills.  rf_render_noalloc serves them:
+the caller passes its own device buffers for the mesh, texture and target,
+and the library's temporaries live in a fixed scratch area compiled into it.
 
 This test calls it through the C ABI twice in a row (plus a third call that
 repeats the first, so nothing left in the shared scratch area by the second
 call can leak), each time on caller-owned device buffers, and checks every
-result against the allocating entry point rf_render: colour, depth and
-stats must match bit for bit, the tolerance all parity tests here use for
-these shaders.  It also checks that inputs beyond the stated limits are
-refused.  The file is named so that pytest collects it last.
+result against the allocating entry point rf_render and against the oracle
+(the reference's CPU path restated): colour, depth and stats must match bit
+for bit, the tolerance all parity tests here use for these shaders.  It also
+checks that inputs beyond the stated limits are refused.  The file is named
+so that pytest collects it last.
 """
 import ctypes as C
 
@@ -23,8 +24,11 @@ import pytest
 import retrofire_gb300 as rf
 from retrofire_gb300 import scenes
 
+from rfhelp import DrawSpec, oracle_render
+
 pytestmark = pytest.mark.gpu
 
+BAD_ARG = 2
 OVER_BUDGET = 5
 
 
@@ -95,20 +99,30 @@ def with_noalloc_entry_point(c):
             rf.Stats.from_c(st).as_dict())
 
 
+def with_oracle(c):
+    """The same frame through the oracle (render.rs:134-207 restated)."""
+    d = DrawSpec(c["verts"], c["faces"], c["shader"], c["mvp"], pos_dim=c["pos_dim"],
+                 tex=c["tex"])
+    return oracle_render([d], c["vp"], c["w"], c["h"])
+
+
 def assert_same(a, b, what):
     assert np.array_equal(a[0], b[0]), what + ": colour differs"
     assert np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32)), what + ": depth differs"
-    assert a[2] == b[2], what + ": stats differ %r vs %r" % (a[2], b[2])
+    sa = {k: a[2][k] for k in b[2]}
+    assert sa == b[2], what + ": stats differ %r vs %r" % (sa, b[2])
 
 
 def test_noalloc_matches_allocating_entry_point_on_consecutive_calls():
     cases = [("textured cube", cube_case()), ("gouraud fill", fill_case()),
              ("textured cube again", cube_case())]
     expected = {name: with_allocating_entry_point(c) for name, c in cases}
+    oracle = {name: with_oracle(c) for name, c in cases}
     for name, c in cases:
         got = with_noalloc_entry_point(c)
         assert got[2]["frags_i"] > 0
-        assert_same(got, expected[name], name)
+        assert_same(got, expected[name], name + " vs rf_render")
+        assert_same(got, oracle[name], name + " vs the oracle")
 
 
 def test_noalloc_refuses_inputs_beyond_its_limits():
@@ -126,3 +140,4 @@ def test_noalloc_refuses_inputs_beyond_its_limits():
     assert call(**dict(args, nverts=4097)) == OVER_BUDGET
     assert call(**dict(args, w=1025)) == OVER_BUDGET
     assert call(**dict(args, h=1025)) == OVER_BUDGET
+    assert call(**dict(args, nverts=0)) == BAD_ARG  # triangles with no vertices
