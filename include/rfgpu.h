@@ -209,9 +209,11 @@ rf_status rf_target_read_async(rf_ctx *ctx, rf_target t, uint32_t *color, float 
 /* ---- rendering -------------------------------------------------------- */
 /* render(mesh.faces, mesh.verts, shader, uniforms, viewport, target, ctx)
  * (render.rs:134-207).  viewport: Mat4<Ndc, Screen>, row-major.  When stats
- * is non-NULL the call waits for completion and stores this call's stats
- * (like `*ctx.stats.borrow_mut() += stats`, render.rs:206); with NULL it
- * only queues the work and the stats accumulate for rf_ctx_take_stats. */
+ * is non-NULL the call waits for the work queued before it and for its own,
+ * and stores this call's stats alone (like `*ctx.stats.borrow_mut() +=
+ * stats`, render.rs:206), which rf_ctx_take_stats then does not report
+ * again; with NULL it only queues the work and the stats accumulate for
+ * rf_ctx_take_stats. */
 rf_status rf_render(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_uniforms *uniforms,
                     const float viewport[16], rf_target target, const rf_context_flags *flags,
                     rf_stats *stats);

@@ -941,6 +941,32 @@ rf_status queue_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, std::vect
     return run_jobs(ctx, in.data(), njobs, true, host);
 }
 
+// The stats of one call made with a stats pointer (render.rs:206 adds them
+// into ctx.stats): the running totals just before and just after the
+// call's work; they are then marked as handed out, so rf_ctx_take_stats
+// does not report them again.
+struct CallStats {
+    rf_stats before{};
+    bool on = false;
+};
+rf_status call_stats_begin(rf_ctx *ctx, const rf_stats *out, CallStats &cs) {
+    if (!out) return RF_OK;
+    rf_status st = init_stats(ctx);
+    if (st) return st;
+    if ((st = read_totals(ctx, cs.before))) return st;
+    cs.on = true;
+    return RF_OK;
+}
+rf_status call_stats_end(rf_ctx *ctx, rf_stats *out, const CallStats &cs) {
+    if (!cs.on) return RF_OK;
+    rf_stats after{};
+    rf_status st = read_totals(ctx, after);
+    if (st) return st;
+    *out = sub_stats(after, cs.before);
+    add_stats(ctx->taken, *out);
+    return RF_OK;
+}
+
 rf_status finish_call(rf_ctx *ctx, rf_stats *out) {
     if (!out) return RF_OK;
     rf_stats tot{};
@@ -1138,6 +1164,8 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
         return RF_ERR_BAD_ARG;
     rf_status st = init_stats(ctx);
     if (st) return st;
+    CallStats cs;
+    if ((st = call_stats_begin(ctx, stats, cs))) return st;
     DrawDev d{};
     d.verts = m.verts;
     d.idx = m.idx;
@@ -1206,7 +1234,7 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
         if (m.async) CK(cudaEventRecord(m.used, s));
         if (tg.async) CK(cudaEventRecord(tg.rendered, s));
     }
-    return finish_call(ctx, stats);
+    return call_stats_end(ctx, stats, cs);
 }
 
 rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const uint32_t *idx) {
@@ -1432,10 +1460,12 @@ rf_status rf_render_draws(rf_ctx *ctx, const rf_draw *draws, uint32_t ndraws,
     ji.vp = viewport;
     ji.tg = &it->second;
     ji.fl = flags;
-    std::vector<JobHost> host;
-    rf_status st = run_jobs(ctx, &ji, 1, false, host);
+    CallStats cs;
+    rf_status st = call_stats_begin(ctx, stats, cs);
     if (st) return st;
-    return finish_call(ctx, stats);
+    std::vector<JobHost> host;
+    if ((st = run_jobs(ctx, &ji, 1, false, host))) return st;
+    return call_stats_end(ctx, stats, cs);
 }
 
 rf_status rf_render_batch(rf_ctx *ctx, const rf_job *jobs, uint32_t njobs, rf_stats *stats) {

@@ -294,6 +294,28 @@ def test_async_stats_accumulate():
     dev.close()
 
 
+def test_call_stats_exclude_queued_work():
+    """A call made with a stats pointer reports its own render() stats only
+    (render.rs:206), even after frames queued without stats; those stay for
+    rf_ctx_take_stats, which does not report the synchronous call again."""
+    draws, vp, w, h = small_fill(seed=24, ntri=400, w=128, h=96)
+    dev = rf.Device()
+    tg = rf.Framebuf(w, h, device=dev)
+    m = rf.Mesh(draws[0].verts, draws[0].faces, pos_dim=4, device=dev)
+    _, _, ost = oracle_render(draws, vp, w, h)
+    for _ in range(2):
+        tg.clear()
+        rf.render_draws([(m, rf.Shader.gouraud(), None)], vp, tg, sync_stats=False)
+    tg.clear()
+    st = rf.render_draws([(m, rf.Shader.gouraud(), None)], vp, tg, sync_stats=True)
+    assert {k: st.as_dict()[k] for k in ost} == ost
+    rest = dev.take_stats()
+    assert rest.calls == 2 and rest.frags_i == 2 * ost["frags_i"]
+    m.close()
+    tg.close()
+    dev.close()
+
+
 def test_bad_arguments():
     dev = rf.Device()
     with pytest.raises(rf.RfError) as e:
