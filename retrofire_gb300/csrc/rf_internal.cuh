@@ -142,7 +142,10 @@ struct RasterPrim {
     uint32_t y0, c0;  // upper half: rows y0 .. y0+c0-1, records 0 .. c0-1
     uint32_t y1, c1;  // lower half: rows y1 .. y1+c1-1, records c0 .. c0+c1-1
     float dvdx[2][RF_NC];
-    uint32_t pad_[3];
+    float zmax;       // >= the depth of every fragment it writes into the target
+                      // (+inf when unknown): a tile whose current depths are all
+                      // >= zmax cannot pass any of them under the Less test
+    uint32_t pad_[2];
 };
 
 // One line after clipping and to_screen (raster.rs:121-173): it steps

@@ -790,6 +790,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     R->draw = di;
                     R->flags = 0u;
                     R->kind = d.shader;
+                    R->zmax = __int_as_float(0x7F800000);
                 }
                 if (!culled) {
                 // This thread's slot: the fields before `runs` only.
@@ -928,6 +929,25 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, const H
     }
 }
 
+// An upper bound of every running sum z_k = z_{k-1} + dz (k < n) of a
+// span starting at z_0 (raster.rs:60-69 / vary.rs:142-155): with dz <= 0
+// the sums never rise, so z_0 itself; with dz > 0, z_0 >= 1e-30 and n <=
+// 2^20 every sum is within (1 + 2^-24)^k of z_0 + k dz and the computed
+// e = fl(z_0 + fl((n - 1) dz)) within (1 - 2^-24)^2 of it, so e times
+// 1 + (n + 5) 2^-23 (exact in f32), rounded, bounds them all.  Otherwise
+// +inf (no bound); NaN inputs give +inf too.
+__device__ __forceinline__ float span_depth_bound(float z0, float dz, uint32_t n) {
+    const float inf = __int_as_float(0x7F800000);
+    if (n == 0) return -inf;
+    if (!(fabsf(z0) < inf) || dz != dz) return inf;
+    if (dz <= 0.0f) return z0;
+    if (!(z0 >= 1e-30f) || n > (1u << 20) || !(dz < inf)) return inf;
+    const float e = fadd(z0, fmul((float)(n - 1u), dz));
+    const float f = fadd(1.0f, fmul((float)(n + 5u), 1.1920928955078125e-07f));  // 1 + (n+5) 2^-23
+    const float b = fmul(e, f);
+    return b == b ? b : inf;
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256, 4)
@@ -970,6 +990,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
     unsigned long long acc_fi = 0, acc_oob = 0;  // per-lane, for cur_job
+    float zhi_tri = -__int_as_float(0x7F800000);  // per-lane bound of this triangle's depths
     uint32_t acc_marks = 0;                        // (triangle, tile) bits set by this lane
     auto flush = [&]() {
         if (cur_job != 0xFFFFFFFFu) {
@@ -1018,6 +1039,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             R->base = 0;
             R->stride = 0;
             R->y0 = R->c0 = R->y1 = R->c1 = 0;
+            R->zmax = __int_as_float(0x7F800000);  // +inf: no bound (only row records give one)
         }
         __syncwarp();
         const PrimRec *P = sP;
@@ -1169,6 +1191,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                                 vb[c] = 0.0f;
                             }
                         }
+                        if (w0) zhi_tri = fmaxf(zhi_tri, span_depth_bound(vb[0], dvc[0], o.px1 - o.px0));
                         switch (nc) {  // only the kind's components step
                             case 1: step_k<1>(vb, dvc, ksteps); break;
                             case 2: step_k<2>(vb, dvc, ksteps); break;
@@ -1186,6 +1209,12 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                     mark_band(band, o, J, word, bit);
                     __syncwarp();
                 }
+                // The triangle's depth bound: the largest of its rows'.
+#pragma unroll
+                for (int sft = 16; sft > 0; sft >>= 1)
+                    zhi_tri = fmaxf(zhi_tri, __shfl_xor_sync(0xFFFFFFFFu, zhi_tri, sft));
+                if (lane == 0) R->zmax = zhi_tri;
+                zhi_tri = -__int_as_float(0x7F800000);
             }
             for (int hh = 0; hh < 2 && !regular; ++hh) {
                 const HalfRec *H = &P->half[hh];

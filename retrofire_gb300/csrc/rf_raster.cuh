@@ -502,6 +502,27 @@ __device__ __forceinline__ void raster_prim(TileCtx &T, const DrawDev *__restric
     }
 }
 
+// FAST path: the least current depth over the tile's rows this warp owns
+// (a lower bound: the segment minima are), warp-uniform.
+template <int TW>
+__device__ __forceinline__ float tile_depth_min(const TileCtx &T) {
+    float m = __int_as_float(0x7F800000);
+    if (T.row_ok)
+        for (uint32_t sg = 0; sg < (uint32_t)TW / RF_SEG; ++sg) m = fminf(m, T.smin[sg * RF_TILE_H + T.lane]);
+#pragma unroll
+    for (int sft = 16; sft > 0; sft >>= 1) m = fminf(m, __shfl_xor_sync(0xFFFFFFFFu, m, sft));
+    return m;
+}
+
+// FAST path: no fragment of triangle R can pass Less in a tile whose depths
+// are all >= tzmin (R->zmax bounds its fragments' depths from above; a NaN
+// on either side never skips).
+template <bool FAST>
+__device__ __forceinline__ bool hidden(const RasterPrim *R, float tzmin) {
+    if constexpr (FAST) return R->zmax <= tzmin;
+    else return false;
+}
+
 // Warp-wide selection of set bits in order: lane L offers the bits b (lane
 // order, then bit order within a word); the first `want` of them go to the
 // output slots first, first + 1, ...  Lane first + k learns where its bit
@@ -936,10 +957,17 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
                 }
             }
         };
+        // FAST: the tile's least current depth (a lower bound of every pixel
+        // a span may write), for skipping whole triangles (RasterPrim::zmax).
+        // Columns past the target's edge hold +inf, so they bound nothing
+        // (they are never written back).
+        float tzmin = 0.0f;
         auto load_tile_and_bounds = [&]() {
             load_tile();
             if constexpr (FAST) {
+                for (uint32_t x = ncols; x < (uint32_t)TW; ++x) sdep[x * RF_TILE_H + lane] = __int_as_float(0x7F800000);
                 for (uint32_t sg = 0; sg < (uint32_t)TW / RF_SEG; ++sg) seg_refresh(T, sg);
+                tzmin = tile_depth_min<TW>(T);
             }
         };
         PrimIter it;
@@ -983,20 +1011,30 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
             wait_staged_but<0>();
 #pragma unroll
             for (int k = 0; k < RA; ++k) {
-                stage_rows<KIND>(T, rslots + k * RW, q[k] != NONE, stage + k, rows);
+                stage_rows<KIND>(T, rslots + k * RW, q[k] != NONE && !hidden<FAST>(stage + k, tzmin), stage + k, rows);
                 commit_stage();
             }
             uint32_t r = 0;  // row slot of t_i (mod RA+1)
             uint32_t h = 0;  // header slot of t_i (mod HA+1)
+            uint32_t visits = 0;  // triangles rasterised (FAST: tzmin refreshed every 8)
             for (;;) {
                 const uint32_t hn = h == 0 ? HS - 1 : h - 1;                // t_{i+HA}: t_{i-1}'s old slot
                 const uint32_t hr = h + RA >= HS ? h + RA - HS : h + RA;    // t_{i+RA}
                 const uint32_t rr = r == 0 ? RS - 1 : r - 1;                // t_{i+RA}: t_{i-1}'s old slot
                 if (q[HA] != NONE) stage_prim(stage + hn, rprims + q[HA], lane);
-                stage_rows<KIND>(T, rslots + rr * RW, q[RA] != NONE, stage + hr, rows);
+                // A triangle whose depth bound is at most the tile's least
+                // depth fails the Less test at every pixel: its rows are not
+                // fetched and its visit is skipped (the tile's depths only rise).
+                stage_rows<KIND>(T, rslots + rr * RW, q[RA] != NONE && !hidden<FAST>(stage + hr, tzmin),
+                                 stage + hr, rows);
                 commit_stage();
                 wait_staged_but<RA>();
-                raster_prim<KIND, FAST>(T, draws, stage + h, prims + q[0], rslots + r * RW);
+                if (!hidden<FAST>(stage + h, tzmin)) {
+                    raster_prim<KIND, FAST>(T, draws, stage + h, prims + q[0], rslots + r * RW);
+                    if constexpr (FAST) {
+                        if ((++visits & 7u) == 0u) tzmin = tile_depth_min<TW>(T);
+                    }
+                }
                 __syncwarp();
                 if (q[1] == NONE) break;
                 const uint32_t qn = q[HA] != NONE ? it.next() : NONE;
