@@ -350,7 +350,7 @@ def batch_leg(args, dev, stream, flush, local):
         workloads.render_per_frame(batch, dev)
 
     b = timed(batched, True)
-    b.update(graphs=True, tile_w=dev.last_tiling()[0], calls_per_step=1)
+    b.update(graphs=True, tile_w=dev.last_tiling()[0], calls_per_step=1)  # (read right after its steps)
     f = timed(per_frame, False)
     f.update(graphs=False, calls_per_step=len(scs))
     peak, peak_kind = measured_peak()
@@ -475,6 +475,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = dev.counts()["kernels"] - k0
+    tiling = dev.last_tiling()  # the timed frames' tile width and warps
     step_ms = [a.elapsed_time(b) for a, b in evs]
     stage, nfr = dev.stage_ms()
     dev.set_timing(False)
@@ -504,7 +505,7 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded fill-rate stress scene)",
-            "config": config({"tile_w": dev.last_tiling()[0], "warps_per_block": dev.last_tiling()[1],
+            "config": config({"tile_w": tiling[0], "warps_per_block": tiling[1],
                               "tiling": "explicit" if args.tile else
                               "online per frame shape, settled before the warm-up"}),
             "tris_per_s": NTRI * args.steps * world / (total_ms / 1e3),
