@@ -84,33 +84,62 @@ RF_HD float fdiv(float a, float b) {
 }
 RF_HD float ffloor(float x) { return floorf(x); }
 
-// Rust `f32 as usize` (64-bit), `as u32`, `as i32`, `as u8`.
+// Rust `f32 as usize` (64-bit), `as u32`, `as i32`, `as u8`: truncation
+// toward zero, saturated to the type's range, NaN to 0.  On the device: a
+// float-to-integer cvt with round-toward-zero, whose results clamp to the
+// destination range; NaN is mapped to 0 first (fmaxf(x, 0) for the unsigned
+// types, which also sends every negative input to 0), since the convert's
+// own NaN result is not 0 for every width.
 RF_HD uint64_t as_usize(float x) {
+#if defined(__CUDA_ARCH__)
+    unsigned long long r;
+    asm("cvt.rzi.u64.f32 %0, %1;" : "=l"(r) : "f"(fmaxf(x, 0.0f)));
+    return r;
+#else
     if (!(x > 0.0f)) return 0;
     if (x >= 18446744073709551616.0f) return UINT64_MAX;
     return (uint64_t)x;
+#endif
 }
 RF_HD uint32_t as_u32(float x);
 // as_usize with the 64-bit conversion only for values that need it.
 RF_HD uint64_t as_usize_fast(float x);
 RF_HD uint32_t as_u32(float x) {
+#if defined(__CUDA_ARCH__)
+    uint32_t r;
+    asm("cvt.rzi.u32.f32 %0, %1;" : "=r"(r) : "f"(fmaxf(x, 0.0f)));
+    return r;
+#else
     if (!(x > 0.0f)) return 0;
     if (x >= 4294967296.0f) return UINT32_MAX;
     return (uint32_t)x;
+#endif
 }
 RF_HD uint64_t as_usize_fast(float x) {
     return x < 4294967296.0f ? (uint64_t)as_u32(x) : as_usize(x);
 }
 RF_HD int32_t as_i32(float x) {
+#if defined(__CUDA_ARCH__)
+    int32_t r;
+    asm("cvt.rzi.s32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return x != x ? 0 : r;
+#else
     if (x != x) return 0;
     if (x <= -2147483648.0f) return INT32_MIN;
     if (x >= 2147483648.0f) return INT32_MAX;
     return (int32_t)x;
+#endif
 }
 RF_HD uint32_t as_u8(float x) {
+#if defined(__CUDA_ARCH__)
+    uint32_t r;
+    asm("cvt.rzi.u8.f32 %0, %1;" : "=r"(r) : "f"(fmaxf(x, 0.0f)));
+    return r & 0xFFu;
+#else
     if (!(x > 0.0f)) return 0;
     if (x >= 255.0f) return 255;
     return (uint32_t)x;
+#endif
 }
 
 // f32::total_cmp key (signed comparison of the returned value).

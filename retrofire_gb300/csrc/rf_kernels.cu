@@ -1318,12 +1318,12 @@ k_tile_items(const JobDev *__restrict__ jobs, uint32_t nj, const uint32_t *__res
         const bool crowded = c > thr;
         // Heavy: more than twice the frame's mean; taken before the rest.
         const bool heavy = crowded || (c > RF_HEAVY_MIN && c > 2ull * *marks / ntiles);
-        items[tile] = heavy ? RF_ITEM_SKIP : tile * 8u;
+        items[tile] = heavy ? RF_ITEM_SKIP : tile << RF_ITEM_SHIFT;
         if (crowded) {
             const uint32_t at = ntiles + atomicAdd(extra, RF_SPLIT_K);
-            for (uint32_t k = 1; k <= RF_SPLIT_K; ++k) items[at + k - 1] = tile * 8u + k;
+            for (uint32_t k = 1; k <= RF_SPLIT_K; ++k) items[at + k - 1] = (tile << RF_ITEM_SHIFT) | k;
         } else if (heavy) {
-            items[ntiles + atomicAdd(extra, 1u)] = tile * 8u;
+            items[ntiles + atomicAdd(extra, 1u)] = tile << RF_ITEM_SHIFT;
         }
     }
 }

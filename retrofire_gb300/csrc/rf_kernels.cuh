@@ -85,16 +85,22 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
 // The rasteriser's work list from the tile masks and the marks total
 // (slots: the warps the rasteriser keeps resident, about).  items (room
 // for (RF_SPLIT_K + 1) * ntiles): items[ntiles .. ntiles + extra) first --
-// heavy tiles (tile * 8) and the row slices of crowded tiles (tile * 8 + k,
-// k = 1 .. RF_SPLIT_K) -- then items[0 .. ntiles): tile t * 8 in index
+// heavy tiles (tile << RF_ITEM_SHIFT) and the row slices of crowded tiles
+// (tile << RF_ITEM_SHIFT | k, k = 1 .. RF_SPLIT_K) -- then items[0 .. ntiles):
+// tile t << RF_ITEM_SHIFT in index
 // order, RF_ITEM_SKIP for the tiles already listed; extra is
 // counters[RF_CNT_ITEMS] (zeroed by launch_setup).
 cudaError_t launch_items(const JobDev *jobs, uint32_t nj, const uint32_t *mask, uint32_t ntiles,
                          const unsigned long long *marks, uint32_t slots, uint32_t *items,
                          uint32_t *counters, cudaStream_t s);
+#ifndef RF_SPLIT_K
 #define RF_SPLIT_K 4  // row slices of a crowded tile (RF_TILE_H / RF_SPLIT_K rows each)
+#endif
+// A work item is tile << RF_ITEM_SHIFT | k (k = 0: the whole tile, 1..RF_SPLIT_K: a slice).
+#define RF_ITEM_SHIFT (RF_SPLIT_K < 8 ? 3u : 4u)
+static_assert(RF_TILE_H % RF_SPLIT_K == 0 && RF_SPLIT_K < 16, "row slices");
 #define RF_ITEM_SKIP 0xFFFFFFFEu  // a work-list entry taken elsewhere in the list
-#define RF_MAX_TILES (1u << 28)  // tiles of one frame or batch (work items hold tile * 8 + k)
+#define RF_MAX_TILES (1u << (31 - RF_ITEM_SHIFT))  // tiles of one frame or batch
 cudaError_t launch_raster(uint32_t tile_w, int kind, bool fast, const JobDev *jobs, uint32_t nj,
                           const DrawDev *draws, const PrimRec *prims, const RasterPrim *rprims,
                           const uint32_t *rows, const uint32_t *tcnt, const uint32_t *toff,

@@ -69,7 +69,7 @@ __device__ uint32_t lshade(const DrawDev &d, const float *v, int32_t fmt) {
         case RF_K_TEX_GOURAUD: c = Kind<RF_K_TEX_GOURAUD>::shade(d, v); break;
         default: c = Kind<RF_K_GOURAUD_SRGB>::shade(d, v); break;
     }
-    return pack_px(c, fmt);
+    return pack_px(c, pack_selector(fmt));
 }
 
 }  // namespace

@@ -30,15 +30,13 @@ namespace rfr {
 using namespace rfx;
 using namespace rfd;
 
-__device__ __forceinline__ uint32_t pack_px(uint32_t c, int32_t fmt) {
-    const uint32_t r = c & 0xFFu, g = (c >> 8) & 0xFFu, b = (c >> 16) & 0xFFu, a = c >> 24;
-    switch (fmt) {  // pixfmt.rs:76-103
-        case RF_K_ARGB8888: return (a << 24) | (r << 16) | (g << 8) | b;
-        case RF_K_XRGB8888: return (r << 16) | (g << 8) | b;
-        case RF_K_RGBA8888: return (r << 24) | (g << 16) | (b << 8) | a;
-        default: return (b << 24) | (g << 16) | (r << 8) | a;
-    }
+// IntoPixel (pixfmt.rs:76-103) of a Color4 packed r | g << 8 | b << 16 |
+// a << 24, as one byte permutation: the selector of each format puts the
+// channels where the format wants them (XRGB8888's top byte is zero).
+__host__ __device__ constexpr uint32_t pack_selector(int32_t fmt) {
+    return fmt == RF_K_ARGB8888 ? 0x3012u : fmt == RF_K_XRGB8888 ? 0x4012u : fmt == RF_K_RGBA8888 ? 0x0123u : 0x2103u;
 }
+__device__ __forceinline__ uint32_t pack_px(uint32_t c, uint32_t sel) { return __byte_perm(c, 0u, sel); }
 
 __device__ __forceinline__ uint32_t to_color4(float r, float g, float b) {
     // color.rs:253-263: (256 * c) as u8, alpha 0xFF.
@@ -130,7 +128,7 @@ struct TileCtx {
     bool has_depth;
     int32_t depth_test;
     bool color_write, depth_write;
-    int32_t fmt;
+    uint32_t fmt;     // pack_selector of the target's pixel format
     unsigned long long frags_o;
 };
 
@@ -898,7 +896,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         }
         item = __shfl_sync(0xFFFFFFFFu, item, 0);
         if (item == 0xFFFFFFFFu) break;
-        const uint32_t tile = item >> 3, slice = item & 7u;  // slice 0: the whole tile
+        const uint32_t tile = item >> RF_ITEM_SHIFT, slice = item & ((1u << RF_ITEM_SHIFT) - 1u);  // 0: the whole tile
         if (tile >= ntiles_total) break;
         const uint32_t ji = upper_index(nj, tile, [&](uint32_t i) { return jobs[i].tile_base; });
         const JobDev &J = jobs[ji];
@@ -920,7 +918,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         T.depth_test = J.depth_test;
         T.color_write = J.color_write != 0;
         T.depth_write = J.depth_write != 0;
-        T.fmt = J.pixfmt;
+        T.fmt = pack_selector(J.pixfmt);
         T.frags_o = 0;
         const uint32_t ncols = T.tx1 - T.tx0;
         const size_t row_off = (size_t)T.y * J.w + T.tx0;
