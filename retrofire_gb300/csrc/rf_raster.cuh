@@ -184,27 +184,51 @@ __device__ __forceinline__ uint32_t pixels(TileCtx &T, const DrawDev &d, float *
                     T.sdep[idx + 3 * RF_TILE_H] = v3[0];
                     ++nout;
                 }
-            } else {
+            } else if constexpr (KIND == RF_K_GOURAUD_SRGB) {
+                // Three powf per pixel: only the passing pixels are shaded.
                 if (p0) {
                     T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
                     T.sdep[idx] = v[0];
-                    ++nout;
                 }
                 if (p1) {
                     T.scol[idx + RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
                     T.sdep[idx + RF_TILE_H] = v1[0];
-                    ++nout;
                 }
                 if (p2) {
                     T.scol[idx + 2 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v2), T.fmt);
                     T.sdep[idx + 2 * RF_TILE_H] = v2[0];
-                    ++nout;
                 }
                 if (p3) {
                     T.scol[idx + 3 * RF_TILE_H] = pack_px(Kind<KIND>::shade(d, v3), T.fmt);
                     T.sdep[idx + 3 * RF_TILE_H] = v3[0];
-                    ++nout;
                 }
+                nout += (uint32_t)p0 + (uint32_t)p1 + (uint32_t)p2 + (uint32_t)p3;
+            } else {
+                // Flat and Gouraud shading are a few instructions and read no
+                // memory: every pixel's colour is computed and only the
+                // stores depend on the depth test (no branches around the
+                // arithmetic).
+                const uint32_t k0 = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                const uint32_t k1 = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
+                const uint32_t k2 = pack_px(Kind<KIND>::shade(d, v2), T.fmt);
+                const uint32_t k3 = pack_px(Kind<KIND>::shade(d, v3), T.fmt);
+                if (p0) {
+                    T.scol[idx] = k0;
+                    T.sdep[idx] = v[0];
+                }
+                if (p1) {
+                    T.scol[idx + RF_TILE_H] = k1;
+                    T.sdep[idx + RF_TILE_H] = v1[0];
+                }
+                if (p2) {
+                    T.scol[idx + 2 * RF_TILE_H] = k2;
+                    T.sdep[idx + 2 * RF_TILE_H] = v2[0];
+                }
+                if (p3) {
+                    T.scol[idx + 3 * RF_TILE_H] = k3;
+                    T.sdep[idx + 3 * RF_TILE_H] = v3[0];
+                }
+                nout += (uint32_t)p0 + (uint32_t)p1 + (uint32_t)p2 + (uint32_t)p3;
             }
 #pragma unroll
             for (int c = 0; c < NC; ++c) v[c] = fadd(v3[c], dv[c]);
@@ -390,6 +414,8 @@ __host__ __device__ constexpr uint32_t row_words(int nc) { return 1u + 2u * (uin
 #define RF_RPW_C0 6
 #define RF_RPW_Y1 7
 #define RF_RPW_C1 8
+#define RF_RPW_ZMAX (9 + 2 * RF_NC)
+static_assert(offsetof(RasterPrim, zmax) == 4 * RF_RPW_ZMAX, "RasterPrim word layout");
 static_assert(offsetof(RasterPrim, flags) == 4 * RF_RPW_FLAGS && offsetof(RasterPrim, base) == 4 * RF_RPW_BASE &&
                   offsetof(RasterPrim, stride) == 4 * RF_RPW_STRIDE && offsetof(RasterPrim, y0) == 4 * RF_RPW_Y0 &&
                   offsetof(RasterPrim, c0) == 4 * RF_RPW_C0 && offsetof(RasterPrim, y1) == 4 * RF_RPW_Y1 &&
@@ -609,6 +635,8 @@ struct PrimIter {
     uint32_t p, pend;
     uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
     uint32_t keep;                // entries of the batch to walk
+    float bz;                     // lane k: entry k's depth bound (RasterPrim::zmax; NaN: none)
+    float zcut;                   // entries whose bound is <= zcut are passed over (NaN: none)
     const RasterPrim *rprims;
     uint32_t slo, shi;            // rows of a row-slice item (slo >= shi: the whole tile)
     bool started, done;           // a window was loaded; the summary words are all read
@@ -697,18 +725,24 @@ struct PrimIter {
         bn = n;
         bi = 0;
         bool take = lane < n;
+        bz = __int_as_float(0x7FFFFFFF);
         if (lane < n) {
             boff = __ldg(toff + mine);
             bcnt = __ldg(tcnt + mine);
-            if (slo < shi && bcnt == 1u) {
-                // A row slice of a crowded tile: an unclipped triangle whose
-                // rows miss the slice is passed over here.
+            if (bcnt == 1u) {
+                // An unclipped triangle: its depth bound, for passing it over
+                // in a tile whose depths have all risen to it (next()) ...
                 const uint32_t *h = reinterpret_cast<const uint32_t *>(rprims + boff);
-                const uint32_t fl = __ldg(h + RF_RPW_FLAGS);
-                const uint32_t y0 = __ldg(h + RF_RPW_Y0), c0 = __ldg(h + RF_RPW_C0);
-                const uint32_t y1 = __ldg(h + RF_RPW_Y1), c1 = __ldg(h + RF_RPW_C1);
-                if (fl & RF_RP_ROWS)
-                    take = (c0 && y0 < shi && y0 + c0 > slo) || (c1 && y1 < shi && y1 + c1 > slo);
+                bz = __ldg(reinterpret_cast<const float *>(h) + RF_RPW_ZMAX);
+                if (slo < shi) {
+                    // ... and, in a row slice of a crowded tile, whether its
+                    // rows meet the slice.
+                    const uint32_t fl = __ldg(h + RF_RPW_FLAGS);
+                    const uint32_t y0 = __ldg(h + RF_RPW_Y0), c0 = __ldg(h + RF_RPW_C0);
+                    const uint32_t y1 = __ldg(h + RF_RPW_Y1), c1 = __ldg(h + RF_RPW_C1);
+                    if (fl & RF_RP_ROWS)
+                        take = (c0 && y0 < shi && y0 + c0 > slo) || (c1 && y1 < shi && y1 + c1 > slo);
+                }
             }
         }
         keep = __ballot_sync(0xFFFFFFFFu, take);
@@ -717,6 +751,7 @@ struct PrimIter {
         sb = s0 = s1 = s2 = s3 = sc = sl = srem = 0;
         widx = wval = wn = wi = wrem = p = pend = 0;
         boff = bcnt = bn = bi = keep = 0;
+        bz = zcut = __int_as_float(0x7FFFFFFF);
         started = done = false;
     }
     __device__ __forceinline__ uint32_t next() {
@@ -725,7 +760,10 @@ struct PrimIter {
                 refill();
                 if (bn == 0) return 0xFFFFFFFFu;
             }
-            if (!((keep >> bi) & 1u)) {
+            // Passed over: entries not kept, and triangles no pixel of the
+            // tile can take any more (depth bound <= the tile's least depth,
+            // which only rises; a NaN on either side never passes over).
+            if (!((keep >> bi) & 1u) || __shfl_sync(0xFFFFFFFFu, bz, bi) <= zcut) {
                 ++bi;
                 continue;
             }
@@ -998,6 +1036,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         if (q[0] != NONE) {
             load_tile_and_bounds();
             loaded = true;
+            if constexpr (FAST) it.zcut = tzmin;
 #pragma unroll
             for (int k = 1; k <= HA; ++k) q[k] = q[k - 1] != NONE ? it.next() : NONE;
             // Headers of t_0 .. t_{HA-1} (t_{HA} comes with G_0), waited
@@ -1030,7 +1069,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
                 if (!hidden<FAST>(stage + h, tzmin)) {
                     raster_prim<KIND, FAST>(T, draws, stage + h, prims + q[0], rslots + r * RW);
                     if constexpr (FAST) {
-                        if ((++visits & 7u) == 0u) tzmin = tile_depth_min<TW>(T);
+                        if ((++visits & 7u) == 0u) it.zcut = tzmin = tile_depth_min<TW>(T);
                     }
                 }
                 __syncwarp();
