@@ -85,11 +85,13 @@ RF_HD float fdiv(float a, float b) {
 RF_HD float ffloor(float x) { return floorf(x); }
 
 // Rust `f32 as usize` (64-bit), `as u32`, `as i32`, `as u8`: truncation
-// toward zero, saturated to the type's range, NaN to 0.  On the device: a
-// float-to-integer cvt with round-toward-zero, whose results clamp to the
-// destination range; NaN is mapped to 0 first (fmaxf(x, 0) for the unsigned
-// types, which also sends every negative input to 0), since the convert's
-// own NaN result is not 0 for every width.
+// toward zero, saturated to the type's range, NaN to 0.  On the device: one
+// float-to-integer cvt with round-toward-zero.  For 8- and 32-bit results
+// it is Rust's `as` by itself on sm_103a (measured: NaN, -NaN, -inf, -1 and
+// -0.9 give 0; 255.9, 1e10 and +inf the type's maximum; the signed form
+// gives INT32_MIN for -inf and 0 for NaN).  The 64-bit unsigned form gives
+// 2^63 for NaN, so as_usize maps NaN (and every negative input) to 0 first
+// with fmaxf(x, 0).
 RF_HD uint64_t as_usize(float x) {
 #if defined(__CUDA_ARCH__)
     unsigned long long r;
@@ -107,7 +109,7 @@ RF_HD uint64_t as_usize_fast(float x);
 RF_HD uint32_t as_u32(float x) {
 #if defined(__CUDA_ARCH__)
     uint32_t r;
-    asm("cvt.rzi.u32.f32 %0, %1;" : "=r"(r) : "f"(fmaxf(x, 0.0f)));
+    asm("cvt.rzi.u32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
 #else
     if (!(x > 0.0f)) return 0;
@@ -122,7 +124,7 @@ RF_HD int32_t as_i32(float x) {
 #if defined(__CUDA_ARCH__)
     int32_t r;
     asm("cvt.rzi.s32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return x != x ? 0 : r;
+    return r;
 #else
     if (x != x) return 0;
     if (x <= -2147483648.0f) return INT32_MIN;
@@ -133,8 +135,8 @@ RF_HD int32_t as_i32(float x) {
 RF_HD uint32_t as_u8(float x) {
 #if defined(__CUDA_ARCH__)
     uint32_t r;
-    asm("cvt.rzi.u8.f32 %0, %1;" : "=r"(r) : "f"(fmaxf(x, 0.0f)));
-    return r & 0xFFu;
+    asm("cvt.rzi.u8.f32 %0, %1;" : "=r"(r) : "f"(x));  // zero-extended to 32 bits
+    return r;
 #else
     if (!(x > 0.0f)) return 0;
     if (x >= 255.0f) return 255;

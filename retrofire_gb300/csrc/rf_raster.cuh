@@ -37,6 +37,23 @@ __host__ __device__ constexpr uint32_t pack_selector(int32_t fmt) {
     return fmt == RF_K_ARGB8888 ? 0x3012u : fmt == RF_K_XRGB8888 ? 0x4012u : fmt == RF_K_RGBA8888 ? 0x0123u : 0x2103u;
 }
 __device__ __forceinline__ uint32_t pack_px(uint32_t c, uint32_t sel) { return __byte_perm(c, 0u, sel); }
+// The same pixel straight from the channel bytes r, g, b (each 0..255 in a
+// 32-bit word): the byte selector over (r | g << 8, b | 0xFF00) -- byte k of
+// the Color4 word is byte {0, 1, 4, 5}[k] there, and byte 2 is a zero.
+__host__ __device__ constexpr uint32_t rgb_selector(uint32_t sel) {
+    uint32_t out = 0;
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t n = (sel >> (4 * i)) & 0xFu;
+        out |= (n == 0u ? 0u : n == 1u ? 1u : n == 2u ? 4u : n == 3u ? 5u : 2u) << (4 * i);
+    }
+    return out;
+}
+static_assert(rgb_selector(0x3012u) == 0x5014u && rgb_selector(0x4012u) == 0x2014u &&
+                  rgb_selector(0x0123u) == 0x0145u && rgb_selector(0x2103u) == 0x4105u,
+              "pixel selectors over the channel bytes");
+__device__ __forceinline__ uint32_t pack_rgb(uint32_t r, uint32_t g, uint32_t b, uint32_t rsel) {
+    return __byte_perm(__byte_perm(r, g, 0x1140u), b | 0xFF00u, rsel);
+}
 
 __device__ __forceinline__ uint32_t to_color4(float r, float g, float b) {
     // color.rs:253-263: (256 * c) as u8, alpha 0xFF.
@@ -88,6 +105,17 @@ struct Kind {
             return t;
         }
     }
+    // shade() packed into the target's pixel format (sel: pack_selector,
+    // rsel: rgb_selector of it).
+    __device__ static __forceinline__ uint32_t shade_px(const DrawDev &d, const float *v, uint32_t sel,
+                                                        uint32_t rsel) {
+        if constexpr (KIND == RF_K_GOURAUD) {
+            // color.rs:253-263 as in to_color4, the bytes permuted at once
+            return pack_rgb(as_u8(fmul(256.0f, v[1])), as_u8(fmul(256.0f, v[2])), as_u8(fmul(256.0f, v[3])), rsel);
+        } else {
+            return pack_px(shade(d, v), sel);
+        }
+    }
     __device__ static __forceinline__ uint32_t shade(const DrawDev &d, const float *v) {
         if constexpr (KIND == RF_K_FLAT) {
             return d.flat_rgba;
@@ -129,6 +157,7 @@ struct TileCtx {
     int32_t depth_test;
     bool color_write, depth_write;
     uint32_t fmt;     // pack_selector of the target's pixel format
+    uint32_t rfmt;    // rgb_selector of fmt
     unsigned long long frags_o;
 };
 
@@ -208,10 +237,10 @@ __device__ __forceinline__ uint32_t pixels(TileCtx &T, const DrawDev &d, float *
                 // memory: every pixel's colour is computed and only the
                 // stores depend on the depth test (no branches around the
                 // arithmetic).
-                const uint32_t k0 = pack_px(Kind<KIND>::shade(d, v), T.fmt);
-                const uint32_t k1 = pack_px(Kind<KIND>::shade(d, v1), T.fmt);
-                const uint32_t k2 = pack_px(Kind<KIND>::shade(d, v2), T.fmt);
-                const uint32_t k3 = pack_px(Kind<KIND>::shade(d, v3), T.fmt);
+                const uint32_t k0 = Kind<KIND>::shade_px(d, v, T.fmt, T.rfmt);
+                const uint32_t k1 = Kind<KIND>::shade_px(d, v1, T.fmt, T.rfmt);
+                const uint32_t k2 = Kind<KIND>::shade_px(d, v2, T.fmt, T.rfmt);
+                const uint32_t k3 = Kind<KIND>::shade_px(d, v3, T.fmt, T.rfmt);
                 if (p0) {
                     T.scol[idx] = k0;
                     T.sdep[idx] = v[0];
@@ -236,7 +265,7 @@ __device__ __forceinline__ uint32_t pixels(TileCtx &T, const DrawDev &d, float *
         for (; idx != end; idx += RF_TILE_H) {
             const float z = v[0];
             if (T.sdep[idx] < z) {
-                T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                T.scol[idx] = Kind<KIND>::shade_px(d, v, T.fmt, T.rfmt);
                 T.sdep[idx] = z;
                 ++nout;
             }
@@ -260,7 +289,7 @@ __device__ __forceinline__ uint32_t pixels(TileCtx &T, const DrawDev &d, float *
             }
             if (pass) {
                 if (T.color_write) {
-                    T.scol[idx] = pack_px(Kind<KIND>::shade(d, v), T.fmt);
+                    T.scol[idx] = Kind<KIND>::shade_px(d, v, T.fmt, T.rfmt);
                     T.frags_o += 1;
                 }
                 if (T.has_depth && T.depth_write) T.sdep[idx] = z;
@@ -633,8 +662,8 @@ struct PrimIter {
     // wn of them; the cursor is entry wi with wrem = its bits not taken yet.
     uint32_t widx, wval, wn, wi, wrem;
     uint32_t p, pend;
-    uint32_t boff, bcnt, bn, bi;  // the gathered batch (lane k: entry k)
-    uint32_t keep;                // entries of the batch to walk
+    uint32_t boff, bcnt, bn;      // the gathered batch (lane k: entry k)
+    uint32_t keep;                // entries of the batch still to walk
     float bz;                     // lane k: entry k's depth bound (RasterPrim::zmax; NaN: none)
     float zcut;                   // entries whose bound is <= zcut are passed over (NaN: none)
     const RasterPrim *rprims;
@@ -723,7 +752,6 @@ struct PrimIter {
         uint32_t mine;
         const uint32_t n = gather_tris(mine);
         bn = n;
-        bi = 0;
         bool take = lane < n;
         bz = __int_as_float(0x7FFFFFFF);
         if (lane < n) {
@@ -745,31 +773,31 @@ struct PrimIter {
                 }
             }
         }
-        keep = __ballot_sync(0xFFFFFFFFu, take);
+        // (entries passed over for their depth bound now are tested again
+        // against the bound of the moment in next())
+        keep = __ballot_sync(0xFFFFFFFFu, take && !(bz <= zcut));
     }
     __device__ __forceinline__ void init() {
         sb = s0 = s1 = s2 = s3 = sc = sl = srem = 0;
         widx = wval = wn = wi = wrem = p = pend = 0;
-        boff = bcnt = bn = bi = keep = 0;
+        boff = bcnt = bn = keep = 0;
         bz = zcut = __int_as_float(0x7FFFFFFF);
         started = done = false;
     }
     __device__ __forceinline__ uint32_t next() {
         while (p >= pend) {
-            if (bi >= bn) {
+            while (keep == 0u) {
                 refill();
                 if (bn == 0) return 0xFFFFFFFFu;
             }
-            // Passed over: entries not kept, and triangles no pixel of the
-            // tile can take any more (depth bound <= the tile's least depth,
-            // which only rises; a NaN on either side never passes over).
-            if (!((keep >> bi) & 1u) || __shfl_sync(0xFFFFFFFFu, bz, bi) <= zcut) {
-                ++bi;
-                continue;
-            }
-            p = __shfl_sync(0xFFFFFFFFu, boff, bi);
-            pend = p + __shfl_sync(0xFFFFFFFFu, bcnt, bi);
-            ++bi;
+            const uint32_t k = __ffs(keep) - 1;
+            keep &= keep - 1u;
+            // Passed over: triangles no pixel of the tile can take any more
+            // (depth bound <= the tile's least depth, which only rises; a
+            // NaN on either side never passes over).
+            if (__shfl_sync(0xFFFFFFFFu, bz, k) <= zcut) continue;
+            p = __shfl_sync(0xFFFFFFFFu, boff, k);
+            pend = p + __shfl_sync(0xFFFFFFFFu, bcnt, k);
         }
         return p++;
     }
@@ -957,6 +985,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         T.color_write = J.color_write != 0;
         T.depth_write = J.depth_write != 0;
         T.fmt = pack_selector(J.pixfmt);
+        T.rfmt = rgb_selector(T.fmt);
         T.frags_o = 0;
         const uint32_t ncols = T.tx1 - T.tx0;
         const size_t row_off = (size_t)T.y * J.w + T.tx0;

@@ -216,6 +216,23 @@ def test_nonfinite_and_w_zero():
     assert_parity(g, o)
 
 
+def test_nonfinite_and_out_of_range_colours():
+    """Colour varyings that are NaN, infinite, negative or above 1: the
+    `(256 * c) as u8` of each channel saturates and takes NaN to 0."""
+    w, h = 96, 64
+    vp = mat.viewport(0, 0, w, h)
+    v = np.array([[-0.9, -0.9, 0.1, 1, np.nan, -1.0, 2.0], [0.9, -0.8, 0.2, 1, 0.5, 3.0, np.inf],
+                  [0.0, 0.9, 0.3, 1, 0.2, -np.inf, 0.5],
+                  [-0.5, 0.5, 0.5, 1, 1e30, -1e30, 0.99], [0.8, 0.8, 0.5, 1, -0.001, 1.01, 0.0],
+                  [0.7, -0.7, 0.5, 1, 0.996, 0.004, -0.0]], np.float32)
+    faces = np.array([[0, 1, 2], [3, 4, 5]], np.uint32)
+    d = DrawSpec(v, faces, rf.GOURAUD, pos_dim=4)
+    for ctx in (rf.Context(face_cull=rf.CULL_NONE), rf.Context(face_cull=rf.CULL_NONE, depth_test=rf.DEPTH_NONE)):
+        g, o = both([d], vp, w, h, ctx=ctx)
+        assert o[2]["frags_o"] > 0
+        assert_parity(g, o)
+
+
 def test_near_plane_and_fullscreen():
     w, h = 400, 300
     vp = mat.viewport(0, 0, w, h)
