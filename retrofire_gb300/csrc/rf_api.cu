@@ -689,7 +689,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                              P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
                              P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
-                             kst, counters, ctx->nsm, s));
+                             kst, counters, ctx->nsm, s, nullptr, nullptr, kind));
         CK(rfk::launch_items(jd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
                              (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));
         CK(mark(RF_STAGE_RASTER));
@@ -793,7 +793,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                              P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
                              P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
-                             kst, counters, ctx->nsm, s, P<uint32_t>(ctx->perm), P<uint32_t>(ctx->ptri)));
+                             kst, counters, ctx->nsm, s, P<uint32_t>(ctx->perm), P<uint32_t>(ctx->ptri), kind));
         CK(rfk::launch_items(vjd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
                              (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));
         CK(mark(RF_STAGE_RASTER));

@@ -950,6 +950,9 @@ __device__ __forceinline__ float span_depth_bound(float z0, float dz, uint32_t n
 
 }  // namespace
 
+// NCT: the components (1 + attributes) of every triangle of the launch, or
+// 0 when its draws mix shader kinds (taken per triangle).
+template <int NCT>
 __global__ void __launch_bounds__(256, 4)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
       PrimRec *__restrict__ prims, const uint32_t *__restrict__ live, uint32_t tile_w,
@@ -1002,12 +1005,8 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     // One band of the target: reduce the lanes' covered columns and mark the
     // band's tiles with this triangle's bit.
     auto mark_band = [&](int64_t band, RowOut &o, const JobDev &J, uint32_t word, uint32_t bit) {
-        uint32_t lo = o.px0 < o.px1 ? o.px0 : 0xFFFFFFFFu, hi = o.px0 < o.px1 ? o.px1 : 0u;
-#pragma unroll
-        for (int sft = 16; sft > 0; sft >>= 1) {
-            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, sft));
-            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, sft));
-        }
+        const uint32_t lo = __reduce_min_sync(0xFFFFFFFFu, o.px0 < o.px1 ? o.px0 : 0xFFFFFFFFu);
+        const uint32_t hi = __reduce_max_sync(0xFFFFFFFFu, o.px0 < o.px1 ? o.px1 : 0u);
         if (lo < hi) {
             const uint32_t t0 = lo >> tw_log2, t1 = (hi - 1) >> tw_log2;
             uint32_t *row = mask + J.mask_base + (size_t)band * J.tiles_x * J.mask_words + word;
@@ -1052,7 +1051,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             const JobDev &J = jobs[job];
             const uint32_t tl = P->tri - J.tri_base;
             const uint32_t word = tl >> 5, bit = 1u << (tl & 31);
-            const uint32_t nc = 1 + nattr_of(P->kind);
+            const uint32_t nc = NCT ? (uint32_t)NCT : 1 + nattr_of(P->kind);
             const uint32_t nr = RF_R_C + nc;
             const uint32_t stride = 1 + 2 * nc;
             bool regular = P->rwords != 0;
@@ -1110,15 +1109,16 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                     R->y1 = (uint32_t)Yh[1];
                     R->c1 = inh[1];
                 }
-                const int64_t lo0 = Yh[0], hi0 = Yh[0] + (int64_t)inh[0] - 1;
-                const int64_t lo1 = Yh[1], hi1 = Yh[1] + (int64_t)inh[1] - 1;
-                const int64_t ylo = inh[0] ? lo0 : lo1, yhi = inh[1] ? hi1 : hi0;
+                // (32-bit rows: a regular triangle's rows are on the target)
+                const int32_t lo0 = (int32_t)Yh[0], hi0 = lo0 + (int32_t)inh[0] - 1;
+                const int32_t lo1 = (int32_t)Yh[1], hi1 = lo1 + (int32_t)inh[1] - 1;
+                const int32_t ylo = inh[0] ? lo0 : lo1, yhi = inh[1] ? hi1 : hi0;
                 float wv0 = lane < nr ? u2f(P->half[0].b0[lane]) : 0.0f;
                 const float wd0 = lane < nr ? P->half[0].d[lane] : 0.0f;
                 float wv1 = lane < nr ? u2f(P->half[1].b0[lane]) : 0.0f;
                 const float wd1 = lane < nr ? P->half[1].d[lane] : 0.0f;
                 // Rows a..b of the band starting at row ys from running value wv.
-                auto walk = [&](float &wv, float wd, int64_t a, int64_t b, int64_t ys) {
+                auto walk = [&](float &wv, float wd, int32_t a, int32_t b, int32_t ys) {
                     if (a > b) return;
                     uint32_t i = (uint32_t)(a - ys);
                     const uint32_t e = (uint32_t)(b - ys) + 1u;
@@ -1135,15 +1135,15 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                         wv = fadd(wv, wd);
                     }
                 };
-                for (int64_t band = (inh[0] | inh[1]) ? ylo / RF_TILE_H : 1; band * RF_TILE_H <= yhi; ++band) {
-                    const int64_t ys = max(ylo, band * RF_TILE_H);
-                    const int64_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
+                for (int32_t band = (inh[0] | inh[1]) ? ylo / RF_TILE_H : 1; band * RF_TILE_H <= yhi; ++band) {
+                    const int32_t ys = max(ylo, band * RF_TILE_H);
+                    const int32_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
                     if (lane < nr) {
                         if (inh[0]) walk(wv0, wd0, max(ys, lo0), min(ye, hi0), ys);
                         if (inh[1]) walk(wv1, wd1, max(ys, lo1), min(ye, hi1), ys);
                     }
                     __syncwarp();
-                    const int64_t y = band * RF_TILE_H + lane;
+                    const int32_t y = band * RF_TILE_H + (int32_t)lane;
                     const bool in0 = inh[0] && y >= lo0 && y <= hi0;
                     const bool in1 = inh[1] && y >= lo1 && y <= hi1;
                     RowOut o{0, 0, 0xFFFFFFFFu, 0};
@@ -1178,9 +1178,10 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                         // The components step side by side (independent
                         // chains), each exactly like Iter::next.
                         const float *dvh = P->half[hh].dvdx;
-                        float vb[RF_NC], dvc[RF_NC];
+                        constexpr uint32_t NCL = NCT ? (uint32_t)NCT : RF_NC;
+                        float vb[NCL], dvc[NCL];
 #pragma unroll
-                        for (uint32_t c = 0; c < RF_NC; ++c) {
+                        for (uint32_t c = 0; c < NCL; ++c) {
                             if (c < nc) {
                                 const float cv = T[i][RF_R_C + c];
                                 dvc[c] = dvh[c];
@@ -1192,16 +1193,20 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                             }
                         }
                         if (w0) zhi_tri = fmaxf(zhi_tri, span_depth_bound(vb[0], dvc[0], o.px1 - o.px0));
-                        switch (nc) {  // only the kind's components step
-                            case 1: step_k<1>(vb, dvc, ksteps); break;
-                            case 2: step_k<2>(vb, dvc, ksteps); break;
-                            case 3: step_k<3>(vb, dvc, ksteps); break;
-                            case 4: step_k<4>(vb, dvc, ksteps); break;
-                            case 5: step_k<5>(vb, dvc, ksteps); break;
-                            default: step_k<6>(vb, dvc, ksteps); break;
+                        if constexpr (NCT != 0) {
+                            step_k<NCT>(vb, dvc, ksteps);
+                        } else {
+                            switch (nc) {  // only the kind's components step
+                                case 1: step_k<1>(vb, dvc, ksteps); break;
+                                case 2: step_k<2>(vb, dvc, ksteps); break;
+                                case 3: step_k<3>(vb, dvc, ksteps); break;
+                                case 4: step_k<4>(vb, dvc, ksteps); break;
+                                case 5: step_k<5>(vb, dvc, ksteps); break;
+                                default: step_k<6>(vb, dvc, ksteps); break;
+                            }
                         }
 #pragma unroll
-                        for (uint32_t c = 0; c < RF_NC; ++c)
+                        for (uint32_t c = 0; c < NCL; ++c)
                             if (c < nc) rec[1 + nc + c] = f2u(vb[c]);
                     }
                     acc_fi += o.frags_i;
@@ -1393,7 +1398,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
                          RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
                          StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
-                         const uint32_t *perm, const uint32_t *ptri) {
+                         const uint32_t *perm, const uint32_t *ptri, int kind) {
     cudaError_t e;
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
@@ -1415,8 +1420,17 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     if (e != cudaSuccess) return e;
     // one warp per live output triangle; the count is only known on the device
     uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
-    k_bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap,
-                                  rprims, mask, stats, counters, marks);
+    auto bin = k_bin<0>;
+    switch (kind) {  // components per triangle: 1 + the kind's attributes
+        case RF_K_FLAT: bin = k_bin<1>; break;
+        case RF_K_TEXTURED: bin = k_bin<3>; break;
+        case RF_K_GOURAUD:
+        case RF_K_GOURAUD_SRGB: bin = k_bin<4>; break;
+        case RF_K_TEX_GOURAUD: bin = k_bin<6>; break;
+        default: break;
+    }
+    bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap, rprims, mask,
+                                stats, counters, marks);
     return cudaGetLastError();
 }
 

@@ -71,7 +71,8 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 // rows_cap words; rows_total receives the words the frame asked for; live
 // (room for every output triangle) receives the indices of the triangles
 // that pass the face-cull test, counters[RF_CNT_LIVE] their number; *marks
-// receives the (triangle, tile) bits set in all.
+// receives the (triangle, tile) bits set in all.  kind: the shader kind of
+// every draw, or RF_K_ANY (the binning kernel is specialised for the first).
 size_t scan64_scratch_words(uint32_t n);
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
@@ -81,7 +82,8 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
                          RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
                          StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
-                         const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr);
+                         const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr,
+                         int kind = RF_K_ANY);
 // The rasteriser's work list from the tile masks and the marks total
 // (slots: the warps the rasteriser keeps resident, about).  items (room
 // for (RF_SPLIT_K + 1) * ntiles): items[ntiles .. ntiles + extra) first --

@@ -261,7 +261,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
                                 triw, trib, scan64, rowtot, rows, ROWS_WORDS, rprims, mask, live,
-                                marks, sd, cnt, nsm, s));
+                                marks, sd, cnt, nsm, s, nullptr, nullptr, shader));
         NA_CK(rfk::launch_items(jd, 1, mask, ntiles, marks, (uint32_t)nsm * 16u, items, cnt, s));
         const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
                           flags->depth_write;
