@@ -696,7 +696,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ tpoly,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
                         uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
-                        uint32_t *__restrict__ live, uint32_t *__restrict__ live_n,
+                        uint2 *__restrict__ live, uint32_t *__restrict__ live_n,
                         uint32_t *__restrict__ extra, StatsDev *__restrict__ stats,
                         const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ptri) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *extra = 0;  // the work list's counter
@@ -851,7 +851,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 uint32_t at = 0;
                 if (lane == lead) at = atomicAdd(live_n, (uint32_t)__popc(bal));
                 at = __shfl_sync(0xFFFFFFFFu, at, lead);
-                if (keep) live[at + __popc(bal & ((1u << lane) - 1u))] = dst;
+                if (keep) live[at + __popc(bal & ((1u << lane) - 1u))] = make_uint2(dst, gt);
             }
             // Write out the records built in this step, one per pass.
             while (bal) {
@@ -955,7 +955,7 @@ __device__ __forceinline__ float span_depth_bound(float z0, float dz, uint32_t n
 template <int NCT>
 __global__ void __launch_bounds__(256, 4)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
-      PrimRec *__restrict__ prims, const uint32_t *__restrict__ live, uint32_t tile_w,
+      PrimRec *__restrict__ prims, const uint2 *__restrict__ live, uint32_t tile_w,
       const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
       unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
       StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
@@ -986,9 +986,13 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     uint32_t cur = 0;
     // Live-list entries: this warp's current and next triangle (the one
     // after that is loaded one iteration ahead).
-    uint32_t pc = wid < nl ? __ldg(live + wid) : 0u;
-    uint32_t pn = wid + nw < nl ? __ldg(live + wid + nw) : 0u;
-    fetch(sbuf[wib][0], pc, wid < nl);
+    // (live entry: the output triangle's index, its input triangle's)
+    uint2 pc = wid < nl ? __ldg(live + wid) : make_uint2(0u, 0u);
+    uint2 pn = wid + nw < nl ? __ldg(live + wid + nw) : make_uint2(0u, 0u);
+    // The current triangle's first row-record word (of its input triangle);
+    // the next one's is loaded an iteration ahead.
+    unsigned long long wbc = wid < nl ? __ldg(tri_wbase + pc.y) : 0ull;
+    fetch(sbuf[wib][0], pc.x, wid < nl);
     RasterPrim *R = &srp[wib];
     float (*T)[RF_NR + 1] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -1021,12 +1025,13 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         }
     };
     for (uint32_t i = wid; i < nl; i += nw) {
-        const uint32_t pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : 0u;
+        const uint2 pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : make_uint2(0u, 0u);
+        const unsigned long long wbn = i + nw < nl ? __ldg(tri_wbase + pn.y) : 0ull;
         __syncwarp();  // the other slot's previous triangle is done
-        fetch(sbuf[wib][cur ^ 1u], pn, i + nw < nl);
+        fetch(sbuf[wib][cur ^ 1u], pn.x, i + nw < nl);
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncwarp();
-        const uint32_t p = pc;
+        const uint32_t p = pc.x;
         pc = pn;
         pn = pnn;
         PrimRec *sP = reinterpret_cast<PrimRec *>(sbuf[wib][cur]);  // fields before `runs` only
@@ -1057,7 +1062,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             bool regular = P->rwords != 0;
             unsigned long long base = 0;
             if (regular) {
-                base = tri_wbase[P->tri] + P->rloc;
+                base = wbc + P->rloc;
                 if (base + P->rwords > rows_cap) {  // no room: rasterise from the PrimRec
                     regular = false;
                     if (lane == 0) atomicAdd(&counters[RF_CNT_ROWSOVF], 1u);
@@ -1271,6 +1276,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             uint4 *dst = reinterpret_cast<uint4 *>(rprims + p);
             if (lane < sizeof(RasterPrim) / 16) dst[lane] = src[lane];
         }
+        wbc = wbn;
     }
     flush();
     warp_add_u64(marks, acc_marks, true);
@@ -1396,7 +1402,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
+                         RasterPrim *rprims, uint32_t *mask, uint2 *live, unsigned long long *marks,
                          StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
                          const uint32_t *perm, const uint32_t *ptri, int kind) {
     cudaError_t e;

@@ -69,8 +69,9 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 // statistics, row records and tile binning (k_bin).  tri_words (nt u32), tri_wbase (nt
 // u64) and scan64 (scan64_scratch_words(nt) u64) are scratch; rows holds
 // rows_cap words; rows_total receives the words the frame asked for; live
-// (room for every output triangle) receives the indices of the triangles
-// that pass the face-cull test, counters[RF_CNT_LIVE] their number; *marks
+// (room for every output triangle) receives, for each triangle that passes
+// the face-cull test, its index and its input triangle's (the record's
+// tri), counters[RF_CNT_LIVE] their number; *marks
 // receives the (triangle, tile) bits set in all.  kind: the shader kind of
 // every draw, or RF_K_ANY (the binning kernel is specialised for the first).
 size_t scan64_scratch_words(uint32_t n);
@@ -80,7 +81,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          PrimRec *prims, uint32_t *tri_words,
                          unsigned long long *tri_wbase, unsigned long long *scan64,
                          unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
+                         RasterPrim *rprims, uint32_t *mask, uint2 *live, unsigned long long *marks,
                          StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
                          const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr,
                          int kind = RF_K_ANY);
