@@ -971,7 +971,9 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     // record is copied (cp.async) while the current one is walked.
     __shared__ __align__(16) uint4 sbuf[8][2][RF_PRIM_CORE_BYTES / 16];  // records' first parts
     __shared__ __align__(16) RasterPrim srp[8];
-    __shared__ float stab[8][32][RF_NR + 1];   // scanline values of one band
+    // Scanline values of one band: quantity q of the band's row i at
+    // [q][i] (rows 16-byte aligned: the walk stores four rows at once).
+    __shared__ __align__(16) float stab[8][RF_NR][RF_TILE_H + 4];
     auto fetch = [&](uint4 *dst, uint32_t p, bool ok) {
         if (ok) {
             const char *src = reinterpret_cast<const char *>(prims + p);
@@ -994,7 +996,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     unsigned long long wbc = wid < nl ? __ldg(tri_wbase + pc.y) : 0ull;
     fetch(sbuf[wib][0], pc.x, wid < nl);
     RasterPrim *R = &srp[wib];
-    float (*T)[RF_NR + 1] = stab[wib];
+    float (*T)[RF_TILE_H + 4] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
     unsigned long long acc_fi = 0, acc_oob = 0;  // per-lane, for cur_job
     float zhi_tri = -__int_as_float(0x7F800000);  // per-lane bound of this triangle's depths
@@ -1122,30 +1124,33 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                 const float wd0 = lane < nr ? P->half[0].d[lane] : 0.0f;
                 float wv1 = lane < nr ? u2f(P->half[1].b0[lane]) : 0.0f;
                 const float wd1 = lane < nr ? P->half[1].d[lane] : 0.0f;
-                // Rows a..b of the band starting at row ys from running value wv.
-                auto walk = [&](float &wv, float wd, int32_t a, int32_t b, int32_t ys) {
+                // Rows a..b of the band starting at row bs from running value wv.
+                auto walk = [&](float &wv, float wd, int32_t a, int32_t b, int32_t bs) {
                     if (a > b) return;
-                    uint32_t i = (uint32_t)(a - ys);
-                    const uint32_t e = (uint32_t)(b - ys) + 1u;
-                    for (; i + 4u <= e; i += 4u) {  // four rows per trip
+                    float *col = T[lane];
+                    uint32_t i = (uint32_t)(a - bs);
+                    const uint32_t e = (uint32_t)(b - bs) + 1u;
+                    for (; (i & 3u) && i < e; ++i) {
+                        col[i] = wv;
+                        wv = fadd(wv, wd);
+                    }
+                    for (; i + 4u <= e; i += 4u) {  // four rows per trip, one store
                         const float w1 = fadd(wv, wd), w2 = fadd(w1, wd), w3 = fadd(w2, wd);
-                        T[i][lane] = wv;
-                        T[i + 1][lane] = w1;
-                        T[i + 2][lane] = w2;
-                        T[i + 3][lane] = w3;
+                        *reinterpret_cast<float4 *>(col + i) = make_float4(wv, w1, w2, w3);
                         wv = fadd(w3, wd);
                     }
                     for (; i < e; ++i) {
-                        T[i][lane] = wv;
+                        col[i] = wv;
                         wv = fadd(wv, wd);
                     }
                 };
                 for (int32_t band = (inh[0] | inh[1]) ? ylo / RF_TILE_H : 1; band * RF_TILE_H <= yhi; ++band) {
                     const int32_t ys = max(ylo, band * RF_TILE_H);
                     const int32_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
+                    const int32_t bs = band * RF_TILE_H;
                     if (lane < nr) {
-                        if (inh[0]) walk(wv0, wd0, max(ys, lo0), min(ye, hi0), ys);
-                        if (inh[1]) walk(wv1, wd1, max(ys, lo1), min(ye, hi1), ys);
+                        if (inh[0]) walk(wv0, wd0, max(ys, lo0), min(ye, hi0), bs);
+                        if (inh[1]) walk(wv1, wd1, max(ys, lo1), min(ye, hi1), bs);
                     }
                     __syncwarp();
                     const int32_t y = band * RF_TILE_H + (int32_t)lane;
@@ -1154,9 +1159,9 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                     RowOut o{0, 0, 0xFFFFFFFFu, 0};
                     if (in0 || in1) {
                         const uint32_t hh = in0 ? 0u : 1u;
-                        const uint32_t i = (uint32_t)(y - ys);
+                        const uint32_t i = (uint32_t)(y - bs);
                         const uint32_t ridx = in0 ? (uint32_t)(y - lo0) : inh[0] + (uint32_t)(y - lo1);
-                        const float lx = T[i][RF_R_LX], rx = T[i][RF_R_RX];
+                        const float lx = T[RF_R_LX][i], rx = T[RF_R_RX][i];
                         const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
                         const uint64_t xs = as_usize_fast(x0r);
                         uint64_t xe = as_usize_fast(x1r);
@@ -1188,7 +1193,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
 #pragma unroll
                         for (uint32_t c = 0; c < NCL; ++c) {
                             if (c < nc) {
-                                const float cv = T[i][RF_R_C + c];
+                                const float cv = T[RF_R_C + c][i];
                                 dvc[c] = dvh[c];
                                 vb[c] = fadd(cv, fmul(fsub(fadd(cv, dvc[c]), cv), tshift));
                                 rec[1 + c] = f2u(vb[c]);
