@@ -89,23 +89,25 @@ RF_HD float ffloor(float x) { return floorf(x); }
 // float-to-integer cvt with round-toward-zero.  For 8- and 32-bit results
 // it is Rust's `as` by itself on sm_103a (measured: NaN, -NaN, -inf, -1 and
 // -0.9 give 0; 255.9, 1e10 and +inf the type's maximum; the signed form
-// gives INT32_MIN for -inf and 0 for NaN).  The 64-bit unsigned form gives
-// 2^63 for NaN, so as_usize maps NaN (and every negative input) to 0 first
-// with fmaxf(x, 0).
+// gives INT32_MIN for -inf and 0 for NaN).  The 64-bit form is built from
+// the 32-bit one and the float's bits instead (the 64-bit convert runs on
+// the FP64 pipe, narrow on this part, and gives 2^63 for NaN): below 2^32
+// -- NaN and negatives included -- the 32-bit convert; from 2^32 (an
+// integer-valued float) its significand shifted into place; from 2^64
+// (+inf too) the maximum.
+RF_HD uint32_t as_u32(float x);
 RF_HD uint64_t as_usize(float x) {
 #if defined(__CUDA_ARCH__)
-    unsigned long long r;
-    asm("cvt.rzi.u64.f32 %0, %1;" : "=l"(r) : "f"(fmaxf(x, 0.0f)));
-    return r;
+    if (!(x >= 4294967296.0f)) return as_u32(x);
+    if (x >= 18446744073709551616.0f) return UINT64_MAX;
+    const uint32_t b = __float_as_uint(x);  // biased exponent 159 .. 190
+    return (uint64_t)((b & 0x7FFFFFu) | 0x800000u) << (((b >> 23) & 0xFFu) - 150u);
 #else
     if (!(x > 0.0f)) return 0;
     if (x >= 18446744073709551616.0f) return UINT64_MAX;
     return (uint64_t)x;
 #endif
 }
-RF_HD uint32_t as_u32(float x);
-// as_usize with the 64-bit conversion only for values that need it.
-RF_HD uint64_t as_usize_fast(float x);
 RF_HD uint32_t as_u32(float x) {
 #if defined(__CUDA_ARCH__)
     uint32_t r;
@@ -116,9 +118,6 @@ RF_HD uint32_t as_u32(float x) {
     if (x >= 4294967296.0f) return UINT32_MAX;
     return (uint32_t)x;
 #endif
-}
-RF_HD uint64_t as_usize_fast(float x) {
-    return x < 4294967296.0f ? (uint64_t)as_u32(x) : as_usize(x);
 }
 RF_HD int32_t as_i32(float x) {
 #if defined(__CUDA_ARCH__)

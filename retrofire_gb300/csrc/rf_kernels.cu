@@ -915,8 +915,8 @@ __device__ __forceinline__ void row_stats(const HalfRec *__restrict__ H, const H
     const float lx = row_value(H, U, RF_R_LX, j);
     const float rx = row_value(H, U, RF_R_RX, j);
     const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-    const uint64_t xs = as_usize_fast(x0r);
-    uint64_t xe = as_usize_fast(x1r);
+    const uint64_t xs = as_usize(x0r);
+    uint64_t xe = as_usize(x1r);
     if (xe < xs) xe = xs;
     o.frags_i += xe - xs;
     if (xe > w) o.oob += 1;
@@ -1095,7 +1095,8 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                     if (lane == 0) acc_oob += 1;
                     continue;
                 }
-                const int64_t Y = (int64_t)fsub(y0r, 0.5f);  // row(j) = max(0, Y + j)
+                // row(j) = max(0, Y + j); |y0r| < 2^22, so the 32-bit convert
+                const int64_t Y = (int32_t)fsub(y0r, 0.5f);
                 // Scanlines at or below the buffer's last row count only in oob.
                 const int64_t in_rows = min((int64_t)n, max((int64_t)0, (int64_t)J.h - Y));
                 if (lane == 0) acc_oob += (unsigned long long)((int64_t)n - in_rows);
@@ -1163,8 +1164,8 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                         const uint32_t ridx = in0 ? (uint32_t)(y - lo0) : inh[0] + (uint32_t)(y - lo1);
                         const float lx = T[RF_R_LX][i], rx = T[RF_R_RX][i];
                         const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-                        const uint64_t xs = as_usize_fast(x0r);
-                        uint64_t xe = as_usize_fast(x1r);
+                        const uint64_t xs = as_usize(x0r);
+                        uint64_t xe = as_usize(x1r);
                         if (xe < xs) xe = xs;
                         o.frags_i = xe - xs;
                         if (xe > J.w) o.oob = 1;
