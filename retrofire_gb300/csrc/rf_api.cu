@@ -27,28 +27,25 @@ struct Mesh {
     uint32_t *idx = nullptr;
     uint32_t nverts = 0, ntri = 0, pos_dim = 3, nattr = 0;  // ntri: lines of a line mesh
     bool lines = false;  // Edge<usize> primitives (index pairs), rf_render_lines
-    // BBox::of the positions (render/scene.rs:37-39): low x,y,z, high x,y,z
-    float bbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    // Device: BBox::of the positions (render/scene.rs:37-39), low x,y,z,
+    // high x,y,z, computed after each upload; then the kernel's scratch
+    // (RF_MESH_BBOX_FLOATS floats in all)
+    float *bbox = nullptr;
     // Asynchronous updates (rf_mesh_update_async): `used` marks the last
     // render that read the mesh, `ready` the end of the last upload.
     bool async = false, ready_pending = false;
     cudaEvent_t used = nullptr, ready = nullptr;
 };
 
-// BBox::extend over every position (f32::min / f32::max, scene.rs:42-46).
-void mesh_bbox(Mesh &m, const float *verts) {
-    for (int k = 0; k < 3; ++k) {
-        m.bbox[k] = INFINITY;
-        m.bbox[3 + k] = -INFINITY;
-    }
-    const uint32_t stride = m.pos_dim + m.nattr;
-    for (uint32_t i = 0; i < m.nverts; ++i)
-        for (int k = 0; k < 3; ++k) {
-            const float x = verts[(size_t)i * stride + k];
-            m.bbox[k] = fminf(m.bbox[k], x);
-            m.bbox[3 + k] = fmaxf(m.bbox[3 + k], x);
-        }
+// Every index below nverts (`vs[i]` panics past the vertices, prim.rs:17-19,
+// 53-55).  A running maximum rather than an early exit, so the loop
+// vectorises.
+bool indices_ok(const uint32_t *idx, uint64_t n, uint32_t nverts) {
+    uint32_t mx = 0;
+    for (uint64_t i = 0; i < n; ++i) mx = idx[i] > mx ? idx[i] : mx;
+    return n == 0 || mx < nverts;
 }
+
 struct Texture {
     uint32_t *texels = nullptr;
     uint32_t w = 0, h = 0;
@@ -430,7 +427,7 @@ rf_status build_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, std::vector<Job
             d.flags = dr.flags & RF_DRAW_CULL_BBOX;
             d.culled = 0;
             d.src_tri_base = (uint32_t)nt;
-            memcpy(d.bbox, m.bbox, sizeof d.bbox);
+            d.bbox = m.bbox;
             memcpy(d.mvp, dr.uniforms.mvp, sizeof d.mvp);
             nv += m.nverts;
             nt += m.ntri;
@@ -894,9 +891,7 @@ rf_status upload_mesh(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t
                       rf_mesh *out) {
     if (!ctx || !out || (pos_dim != 3 && pos_dim != 4) || nattr > RF_MAX_ATTR) return RF_ERR_BAD_ARG;
     if ((nverts && !verts) || (nprim && !idx)) return RF_ERR_BAD_ARG;
-    // `vs[i]` would panic on an index past the vertices (prim.rs:17-19, 53-55)
-    for (uint64_t i = 0; i < (uint64_t)per * nprim; ++i)
-        if (idx[i] >= nverts) return RF_ERR_BAD_ARG;
+    if (!indices_ok(idx, (uint64_t)per * nprim, nverts)) return RF_ERR_BAD_ARG;
     Mesh m;
     m.nverts = nverts;
     m.ntri = nprim;
@@ -907,15 +902,17 @@ rf_status upload_mesh(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t
     cudaError_t e = cudaSuccess;
     if (vb) e = cudaMalloc(&m.verts, vb);
     if (e == cudaSuccess && ib) e = cudaMalloc(&m.idx, ib);
+    if (e == cudaSuccess) e = cudaMalloc(&m.bbox, RF_MESH_BBOX_FLOATS * 4);
     if (e == cudaSuccess && vb) e = cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && ib) e = cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = rfk::launch_mesh_bbox(m.verts, nverts, pos_dim + nattr, m.bbox, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         cudaFree(m.verts);
         cudaFree(m.idx);
+        cudaFree(m.bbox);
         return cuda_fail(ctx, e, per == 2 ? "rf_lines_upload" : "rf_mesh_upload");
     }
-    mesh_bbox(m, verts);
     const uint64_t h = ctx->next_handle++;
     ctx->res->meshes[h] = m;
     *out = h;
@@ -1037,7 +1034,12 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     if (!ctx) return RF_ERR_BAD_ARG;
     sync_all(ctx);
     if (!ctx->shared_res) {
-        for (auto &kv : ctx->res->meshes) { cudaFree(kv.second.verts); cudaFree(kv.second.idx); drop_async(kv.second); }
+        for (auto &kv : ctx->res->meshes) {
+            cudaFree(kv.second.verts);
+            cudaFree(kv.second.idx);
+            cudaFree(kv.second.bbox);
+            drop_async(kv.second);
+        }
         for (auto &kv : ctx->res->textures) cudaFree(kv.second.texels);
     }
     for (auto &kv : ctx->targets) { cudaFree(kv.second.color); cudaFree(kv.second.depth); drop_async(kv.second); }
@@ -1169,6 +1171,7 @@ rf_status rf_render_lines(rf_ctx *ctx, rf_mesh mesh, int32_t shader, const rf_un
     DrawDev d{};
     d.verts = m.verts;
     d.idx = m.idx;
+    d.bbox = m.bbox;
     d.nverts = m.nverts;
     d.ntri = m.ntri;
     d.pos_dim = m.pos_dim;
@@ -1243,16 +1246,14 @@ rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const ui
     if (it == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = it->second;
     const uint32_t per = m.lines ? 2u : 3u;
-    if (idx)
-        for (uint64_t i = 0; i < (uint64_t)per * m.ntri; ++i)
-            if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
+    if (idx && !indices_ok(idx, (uint64_t)per * m.ntri, m.nverts)) return RF_ERR_BAD_ARG;
     const size_t vb = (size_t)m.nverts * (m.pos_dim + m.nattr) * 4, ib = (size_t)m.ntri * per * 4;
     rf_status st = before_use(ctx, m);  // an asynchronous upload still in flight
     if (st) return st;
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
+    if (verts) CK(rfk::launch_mesh_bbox(m.verts, m.nverts, m.pos_dim + m.nattr, m.bbox, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    if (verts) mesh_bbox(m, verts);
     return RF_OK;
 }
 
@@ -1262,9 +1263,7 @@ rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, co
     if (it == ctx->res->meshes.end()) return RF_ERR_BAD_HANDLE;
     Mesh &m = it->second;
     const uint32_t per = m.lines ? 2u : 3u;
-    if (idx)
-        for (uint64_t i = 0; i < (uint64_t)per * m.ntri; ++i)
-            if (idx[i] >= m.nverts) return RF_ERR_BAD_ARG;
+    if (idx && !indices_ok(idx, (uint64_t)per * m.ntri, m.nverts)) return RF_ERR_BAD_ARG;
     rf_status st = copy_streams(ctx);
     if (st) return st;
     if ((st = make_async(ctx, m))) return st;
@@ -1273,9 +1272,9 @@ rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, co
     CK(cudaStreamWaitEvent(ctx->up, m.used, 0));
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->up));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->up));
+    if (verts) CK(rfk::launch_mesh_bbox(m.verts, m.nverts, m.pos_dim + m.nattr, m.bbox, ctx->up));
     CK(cudaEventRecord(m.ready, ctx->up));
     m.ready_pending = true;
-    if (verts) mesh_bbox(m, verts);
     return RF_OK;
 }
 
@@ -1297,6 +1296,7 @@ rf_status rf_mesh_destroy(rf_ctx *ctx, rf_mesh mesh) {
     if (st) return st;
     cudaFree(it->second.verts);
     cudaFree(it->second.idx);
+    cudaFree(it->second.bbox);
     drop_async(it->second);
     ctx->res->meshes.erase(it);
     return RF_OK;

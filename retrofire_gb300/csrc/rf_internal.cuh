@@ -39,7 +39,7 @@ struct DrawDev {
     uint32_t src_tri_base;  // first global input triangle (== tri_base except in a
                             // depth-sorted frame's setup, where tri_base counts
                             // clipped triangles)
-    float bbox[6];    // BBox::of the positions: low x,y,z, high x,y,z
+    const float *bbox;  // BBox::of the positions (device): low x,y,z, high x,y,z
     float mvp[16];
 };
 

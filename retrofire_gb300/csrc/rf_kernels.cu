@@ -98,6 +98,54 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
 }
 
 // ---------------------------------------------------------------------------
+// A mesh's BBox::of (render/scene.rs:37-46: BBox::extend over every
+// position, f32::min / f32::max) on the device, after each upload: block b
+// folds vertices b, b + nb, ... into part[b]; one block then folds the
+// parts into out.  min/max ignore a NaN operand and their result does not
+// depend on the order (up to the sign of a zero, which no cull test sees).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_bbox_part(const float *__restrict__ verts, uint32_t nverts,
+                                                   uint32_t stride, float *__restrict__ part) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nverts; i += gridDim.x * blockDim.x) {
+        const float *v = verts + (size_t)i * stride;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], v[k]);
+            hi[k] = fmaxf(hi[k], v[k]);
+        }
+    }
+    __shared__ float red[6][8];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
+        }
+        if (lane == 0) {
+            red[k][w] = lo[k];
+            red[3 + k][w] = hi[k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        float r = red[threadIdx.x][0];
+        for (uint32_t j = 1; j < blockDim.x / 32; ++j)
+            r = threadIdx.x < 3 ? fminf(r, red[threadIdx.x][j]) : fmaxf(r, red[threadIdx.x][j]);
+        part[blockIdx.x * 6 + threadIdx.x] = r;
+    }
+}
+__global__ void k_bbox_fold(const float *__restrict__ part, uint32_t nb, float *__restrict__ out) {
+    if (threadIdx.x < 6) {
+        float r = threadIdx.x < 3 ? INFINITY : -INFINITY;
+        for (uint32_t b = 0; b < nb; ++b)
+            r = threadIdx.x < 3 ? fminf(r, part[b * 6 + threadIdx.x]) : fmaxf(r, part[b * 6 + threadIdx.x]);
+        out[threadIdx.x] = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // K0: object-level frustum culling (render/scene.rs:80-87 BBox::visibility
 // as the per-object loop of demos/src/bin/crates.rs:114-133 uses it): one
 // thread per draw with RF_DRAW_CULL_BBOX.  The bbox corners in BBox::verts
@@ -1395,6 +1443,14 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
         k_scan_sums<<<1, 1024, 0, s>>>(scratch, nb, total);
         k_scan_add<<<nb, SCAN_THREADS, 0, s>>>(out, n, scratch);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_bbox(const float *verts, uint32_t nverts, uint32_t stride, float *bbox,
+                             cudaStream_t s) {
+    const uint32_t nb = max(1u, min(RF_MESH_BBOX_BLOCKS, (nverts + 255) / 256));
+    k_bbox_part<<<nb, 256, 0, s>>>(verts, nverts, stride, bbox + 6);
+    k_bbox_fold<<<1, 32, 0, s>>>(bbox + 6, nb, bbox);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,13 @@ cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
                         const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, uint32_t *queue,
                         PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s);
+// BBox::of a mesh's positions (the first three floats of each vertex of
+// stride floats) into bbox[0..6); bbox[6 ..) is scratch for the per-block
+// parts: bbox holds RF_MESH_BBOX_FLOATS floats.
+#define RF_MESH_BBOX_BLOCKS 64u
+#define RF_MESH_BBOX_FLOATS (6u + 6u * RF_MESH_BBOX_BLOCKS)
+cudaError_t launch_mesh_bbox(const float *verts, uint32_t nverts, uint32_t stride, float *bbox,
+                             cudaStream_t s);
 size_t scan_scratch_words(uint32_t n);
 cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch,
                         uint32_t *total, cudaStream_t s);
