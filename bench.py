@@ -488,6 +488,10 @@ def run_gpu(args):
         e2e = run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world)
 
     bleg = sleg = None
+    others = {}
+    if rank == 0 and not args.no_others:
+        for name in ("cube", "cubes"):
+            others[name] = workload_leg(args, name, stream, flush, local)
     if rank == 0 and not args.no_batch:
         bleg = batch_leg(args, dev, stream, flush, local)
     if rank == 0 and not args.no_serve:
@@ -522,6 +526,8 @@ def run_gpu(args):
             "clocks": clk,
             "batch": bleg,
             "serve": sleg,
+            "cube": others.get("cube"),
+            "cubes": others.get("cubes"),
         }
         print(json.dumps(line))
     for o in (mesh, tg):
@@ -609,6 +615,72 @@ def device_time(dev, stream, step, steps, warmup, flush, local, stages=True):
     return step_ms, {k: v / max(nfr, 1) for k, v in stage.items()}, launches, clk
 
 
+def measure_workload(args, name, scs, dev, stream, flush, local, world):
+    """Upload one of the further configurations (C1 cube / C3 cubes / C4
+    batch) to dev and time it: per-step device times with CUDA events, the
+    stage times, and the streamed end-to-end seconds.  The caller closes
+    the returned scenes (objs) and turns the seconds into a rate."""
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import workloads
+    objs = workloads.upload(scs, dev)
+    batch = objs["scenes"]
+    st = rf.render_batch(batch, device=dev)  # per-scene stats of one step
+    frags_i = sum(x.frags_i for x in st)
+    frags_o = sum(x.frags_o for x in st)
+    px = sum(sc["w"] * sc["h"] for sc in scs)
+    graphs = name == "cube"
+    if graphs:
+        dev.set_graphs(True)
+
+    def step():
+        for tg in objs["targets"]:
+            tg.clear()
+        rf.render_batch(batch, device=dev, sync_stats=False)
+
+    if not args.tile:
+        for _ in range(TUNE_FRAMES):  # online tiling settles (setup, untimed)
+            step()
+    if world > 1:
+        import torch
+        torch.distributed.barrier()
+    step_ms, stage, launches, clk = device_time(dev, stream, step, args.steps, args.warmup,
+                                                flush, local, stages=not graphs)
+    e2e = None
+    if not args.no_e2e:
+        objs2 = workloads.upload(scs, dev)  # a second device copy to stream over
+        e2e = workloads.e2e(objs, dev, args.steps, max(1, args.warmup), objs2)
+        workloads.close(objs2)
+    return {"objs": objs, "frags_i": frags_i, "frags_o": frags_o, "px": px, "graphs": graphs,
+            "step_ms": step_ms, "stage": stage, "launches": launches, "clk": clk, "e2e": e2e}
+
+
+def workload_leg(args, name, stream, flush, local):
+    """The default line's summary of C1 (textured cube) or C3 (instanced
+    cubes) on a fresh device of its own: device time per frame, the raster
+    stage, and the streamed end-to-end rate with one synchronous frame's
+    latency."""
+    import retrofire_gb300 as rf
+    from retrofire_gb300 import workloads
+    dev = rf.Device(stream.cuda_stream)
+    scs = workloads.scenes_for(name)
+    m = measure_workload(args, name, scs, dev, stream, flush, local, 1)
+    ms = sum(m["step_ms"]) / len(m["step_ms"])
+    out = {"workload": workloads.describe(name)["workload"], "graphs": m["graphs"],
+           "tile_w": dev.last_tiling()[0], "ms_per_frame": ms,
+           "frags_per_s": m["frags_i"] / (ms / 1e3), "frags_i_per_frame": m["frags_i"],
+           "raster_ms": m["stage"].get("raster") if m["stage"] and not m["graphs"] else None,
+           "gpu_launches_per_frame": m["launches"] / max(1, args.steps), "clocks": m["clk"]}
+    e2e = m["e2e"]
+    if e2e is not None:
+        out["e2e"] = {"frags_per_s": m["frags_i"] * args.steps / e2e.pop("seconds"),
+                      "latency_ms": e2e.get("latency_ms"),
+                      "h2d_bytes_per_frame": e2e.get("h2d_bytes_per_step"),
+                      "d2h_bytes_per_frame": e2e.get("d2h_bytes_per_step")}
+    workloads.close(m["objs"])
+    dev.close()
+    return out
+
+
 def run_workload(args):
     """C1 cube / C3 cubes / C4 batch on one GPU (replicas for N > 1)."""
     import numpy as np
@@ -634,36 +706,12 @@ def run_workload(args):
     dev = rf.Device(stream.cuda_stream)
     if args.tile or args.warps:
         dev.set_tiling(args.tile, args.warps)
-    objs = workloads.upload(scs, dev)
-    batch = objs["scenes"]
-    st = rf.render_batch(batch, device=dev)  # per-scene stats of one step
-    frags_i = sum(x.frags_i for x in st)
-    frags_o = sum(x.frags_o for x in st)
-    px = sum(sc["w"] * sc["h"] for sc in scs)
-    graphs = name == "cube"
-    if graphs:
-        dev.set_graphs(True)
     flush = None if args.no_flush else torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-
-    def step():
-        for tg in objs["targets"]:
-            tg.clear()
-        rf.render_batch(batch, device=dev, sync_stats=False)
-
-    if not args.tile:
-        for _ in range(TUNE_FRAMES):  # online tiling settles (setup, untimed)
-            step()
-
-    if world > 1:
-        torch.distributed.barrier()
-    step_ms, stage, launches, clk = device_time(dev, stream, step, args.steps, args.warmup,
-                                                flush, local, stages=not graphs)
+    m = measure_workload(args, name, scs, dev, stream, flush, local, world)
+    objs, frags_i, frags_o, px, graphs = m["objs"], m["frags_i"], m["frags_o"], m["px"], m["graphs"]
+    step_ms, stage, launches, clk, e2e = m["step_ms"], m["stage"], m["launches"], m["clk"], m["e2e"]
     total_ms = max_over_ranks(sum(step_ms), world, "cuda")
-    e2e = None
-    if not args.no_e2e:
-        objs2 = workloads.upload(scs, dev)  # a second device copy to stream over
-        e2e = workloads.e2e(objs, dev, args.steps, max(1, args.warmup), objs2)
-        workloads.close(objs2)
+    if e2e is not None:
         e2e_ms = max_over_ranks(1e3 * e2e.pop("seconds"), world, "cuda")
         e2e["value"] = replica_rate(frags_i * args.steps, world, e2e_ms)
         e2e["unit"] = "frags/s"
@@ -801,6 +849,8 @@ def main():
     ap.add_argument("--inflight", type=int, default=2, help="serving pipelines")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-per-frame leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-per-frame leg")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the default line's textured-cube and instanced-cubes legs")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # --gpus N without a launcher: start N replicas (one process per GPU)
