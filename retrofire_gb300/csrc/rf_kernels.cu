@@ -1169,14 +1169,17 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                 const int32_t lo0 = (int32_t)Yh[0], hi0 = lo0 + (int32_t)inh[0] - 1;
                 const int32_t lo1 = (int32_t)Yh[1], hi1 = lo1 + (int32_t)inh[1] - 1;
                 const int32_t ylo = inh[0] ? lo0 : lo1, yhi = inh[1] ? hi1 : hi0;
-                float wv0 = lane < nr ? u2f(P->half[0].b0[lane]) : 0.0f;
-                const float wd0 = lane < nr ? P->half[0].d[lane] : 0.0f;
-                float wv1 = lane < nr ? u2f(P->half[1].b0[lane]) : 0.0f;
-                const float wd1 = lane < nr ? P->half[1].d[lane] : 0.0f;
+                // Lane q (< nr) runs the upper half's quantity q, lane 16 + q
+                // the lower half's, so a band holding both walks them at once.
+                const uint32_t wq = lane & 15u, wh = lane >> 4;
+                const bool wlane = wq < nr && (wh ? inh[1] : inh[0]) != 0u;
+                float wv = wlane ? u2f(P->half[wh].b0[wq]) : 0.0f;
+                const float wd = wlane ? P->half[wh].d[wq] : 0.0f;
+                const int32_t wlo = wh ? lo1 : lo0, whi = wh ? hi1 : hi0;
                 // Rows a..b of the band starting at row bs from running value wv.
                 auto walk = [&](float &wv, float wd, int32_t a, int32_t b, int32_t bs) {
                     if (a > b) return;
-                    float *col = T[lane];
+                    float *col = T[wq];
                     uint32_t i = (uint32_t)(a - bs);
                     const uint32_t e = (uint32_t)(b - bs) + 1u;
                     for (; (i & 3u) && i < e; ++i) {
@@ -1197,10 +1200,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                     const int32_t ys = max(ylo, band * RF_TILE_H);
                     const int32_t ye = min(yhi, band * RF_TILE_H + RF_TILE_H - 1);
                     const int32_t bs = band * RF_TILE_H;
-                    if (lane < nr) {
-                        if (inh[0]) walk(wv0, wd0, max(ys, lo0), min(ye, hi0), bs);
-                        if (inh[1]) walk(wv1, wd1, max(ys, lo1), min(ye, hi1), bs);
-                    }
+                    if (wlane) walk(wv, wd, max(ys, wlo), min(ye, whi), bs);
                     __syncwarp();
                     const int32_t y = band * RF_TILE_H + (int32_t)lane;
                     const bool in0 = inh[0] && y >= lo0 && y <= hi0;
