@@ -10,6 +10,9 @@ Context.  A step = Frame::clear + one render() of the whole mesh.
 value   fragments (Stats.frags.i) per second with the mesh resident in HBM,
         timed with CUDA events around each step on the library's stream; an
         L2 flush (512 MiB write) runs between steps, outside the timed span.
+        The frame's launches are replayed as one CUDA graph; the stage times
+        and the roofline come from as many steps before them with the
+        library's per-stage events (those run without replay).
 e2e     the same metric through the C ABI with host buffers: per step the
         mesh is uploaded from pinned host memory, the target cleared and
         rendered, and its colour + depth read back to pinned memory; steps
@@ -257,6 +260,7 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
 
     dev2 = rf.Device()
     dev2.set_tiling(*dev.last_tiling())  # the tile width the first context settled on
+    dev2.set_graphs(True)  # both contexts replay each frame's launches as one graph
     own = []  # the objects created here (closed at the end)
     slots = []  # (device, mesh, target, pinned outputs): frames alternate devices
     for b in range(2):
@@ -319,8 +323,8 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
             "h2d_bytes_per_step": int(s["verts"].nbytes + s["faces"].nbytes),
             "d2h_bytes_per_step": int(2 * 4 * W * H),
             "mode": "streamed over two contexts (two CUDA streams) with two device meshes and "
-                    "targets each, async copies on the contexts' copy streams, wall clock to "
-                    "the final sync",
+                    "targets each, async copies on the contexts' copy streams, CUDA graph "
+                    "replay, wall clock to the final sync",
             "latency_ms": {"p50": lat_ms[len(lat_ms) // 2],
                            "p99": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
                            "note": "one synchronous step on one context: upload, render, "
@@ -482,33 +486,48 @@ def run_gpu(args):
     if not args.tile:
         for _ in range(TUNE_FRAMES):  # online tiling settles (setup, untimed)
             step()
+    def timed(n, stage_events):
+        """n steps, each bracketed by CUDA events on the library's stream,
+        the L2 flushed before each; with stage_events the library also
+        records its per-stage events (which turns graph replay off)."""
+        dev.set_timing(stage_events)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(n)]
+        clocks = Clocks(local)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        k0 = dev.counts()["kernels"]
+        clocks.start()
+        with torch.cuda.stream(stream):
+            for i in range(n):
+                if flush is not None:
+                    flush.fill_(i & 0xFF)
+                evs[i][0].record(stream)
+                step()
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        launches = dev.counts()["kernels"] - k0
+        stage = dev.stage_ms() if stage_events else None
+        dev.set_timing(False)
+        return [a.elapsed_time(b) for a, b in evs], launches, clk, stage
+
+    # Per-stage CUDA events first (the raster kernel's time for the
+    # roofline), then the timed steps proper with graph replay: the frame's
+    # launch sequence is captured once and replayed by one graph launch.
     for _ in range(args.warmup):
         step()
     dev.sync()
     dev.stage_ms()  # discard warm-up timings
-    dev.set_timing(True)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    clocks = Clocks(local)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    k0 = dev.counts()["kernels"]
-    clocks.start()
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            if flush is not None:
-                flush.fill_(i & 0xFF)
-            evs[i][0].record(stream)
-            step()
-            evs[i][1].record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    launches = dev.counts()["kernels"] - k0
+    _, _, _, (stage, nfr) = timed(args.steps, True)
     tiling = dev.last_tiling()  # the timed frames' tile width and warps
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    stage, nfr = dev.stage_ms()
-    dev.set_timing(False)
+    dev.set_graphs(True)
+    for _ in range(args.warmup):
+        step()
+    g0 = dev.counts()["graph_launches"]
+    step_ms, launches, clk, _ = timed(args.steps, False)
+    graph_launches = dev.counts()["graph_launches"] - g0
     total_ms = max_over_ranks(sum(step_ms), world, "cuda")
     ms = total_ms / args.steps
     value = replica_rate(frags_i * args.steps, world, total_ms)
@@ -541,7 +560,12 @@ def run_gpu(args):
             "dtype": "f32", "data": "synthetic (seeded fill-rate stress scene)",
             "config": config({"tile_w": tiling[0], "warps_per_block": tiling[1],
                               "tiling": "explicit" if args.tile else
-                              "online per frame shape, settled before the warm-up"}),
+                              "online per frame shape, settled before the warm-up",
+                              "launch": "CUDA graph replay of the frame (%d graph launches "
+                                        "in the timed steps); the stage times and the "
+                                        "roofline come from as many steps before them with "
+                                        "per-stage events, which run without replay"
+                                        % graph_launches}),
             "tris_per_s": NTRI * args.steps * world / (total_ms / 1e3),
             "frames_per_s": args.steps * world / (total_ms / 1e3),
             "frags_o_per_frame": frags_o, "frags_i_per_frame": frags_i,
