@@ -70,6 +70,7 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
             counters[RF_CNT_POOL] = 0;
             counters[RF_CNT_QUEUE] = 0;
             counters[RF_CNT_LIVE] = 0;
+            counters[RF_CNT_LIVE_SMALL] = 0;
             counters[RF_CNT_CLIPQ] = 0;
             *marks = 0;
         }
@@ -745,6 +746,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
                         uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
                         uint2 *__restrict__ live, uint32_t *__restrict__ live_n,
+                        uint2 *__restrict__ live_small, uint32_t *__restrict__ live_small_n,
                         uint32_t *__restrict__ extra, StatsDev *__restrict__ stats,
                         const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ptri) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *extra = 0;  // the work list's counter
@@ -793,6 +795,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
         for (uint32_t c = 0; c < maxc; ++c) {
             const bool have = c < cnt;
             bool keep = false;  // passes the face-cull test
+            bool small = false;  // ... and goes to the small list (k_bin_small)
             if (have) {
                 const DrawDev &d = draws[di];
                 const JobDev &J = jobs[job];
@@ -884,6 +887,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     P.rwords = (uint32_t)w;
                     words += (uint32_t)w;
                 }
+                small = P.rwords != 0u && rows <= RF_SMALL_ROWS;
                 if (P.rwords == 0u) {  // rasterised from this record: it needs the runs
                     PrimRec *G = prims + p0 + c;
                     for (int hh = 0; hh < 2; ++hh)
@@ -894,12 +898,17 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
             __syncwarp();
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
             const uint32_t dst = p0 + c;
-            if (bal) {  // append this step's live triangles to the list
-                const uint32_t lead = __ffs(bal) - 1;
+            // Append this step's live triangles to their lists.
+            const uint32_t bsm = __ballot_sync(0xFFFFFFFFu, keep && small);
+            for (int which = 0; which < 2; ++which) {
+                const uint32_t b = which ? bsm : bal & ~bsm;
+                if (!b) continue;
+                const uint32_t lead = __ffs(b) - 1;
                 uint32_t at = 0;
-                if (lane == lead) at = atomicAdd(live_n, (uint32_t)__popc(bal));
+                if (lane == lead) at = atomicAdd(which ? live_small_n : live_n, (uint32_t)__popc(b));
                 at = __shfl_sync(0xFFFFFFFFu, at, lead);
-                if (keep) live[at + __popc(bal & ((1u << lane) - 1u))] = make_uint2(dst, gt);
+                if ((b >> lane) & 1u)
+                    (which ? live_small : live)[at + __popc(b & ((1u << lane) - 1u))] = make_uint2(dst, gt);
             }
             // Write out the records built in this step, one per pass.
             while (bal) {
@@ -994,6 +1003,72 @@ __device__ __forceinline__ float span_depth_bound(float z0, float dz, uint32_t n
     const float f = fadd(1.0f, fmul((float)(n + 5u), 1.1920928955078125e-07f));  // 1 + (n+5) 2^-23
     const float b = fmul(e, f);
     return b == b ? b : inf;
+}
+
+// One scanline of a regular triangle (raster.rs:84-113): its span from the
+// row's edge values lx, rx (target.rs:259-264 for frags.i / oob), its row
+// record at rec -- w0 = first | end << 16 of the covered columns, the
+// varyings at the first fragment, then at the span's first tile boundary
+// -- and the bound of its depths into zhi.  cv[c * cs] is component c of
+// the row's interpolated values; dvh the half's per-pixel steps.
+template <int NCT>
+__device__ __forceinline__ void row_record(float lx, float rx, const float *cv, uint32_t cs,
+                                           const float *dvh, uint32_t nc, uint32_t w, uint32_t tile_w,
+                                           uint32_t *rec, RowOut &o, float &zhi) {
+    const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
+    const uint64_t xs = as_usize(x0r);
+    uint64_t xe = as_usize(x1r);
+    if (xe < xs) xe = xs;
+    o.frags_i = xe - xs;
+    if (xe > w) o.oob = 1;
+    uint64_t nfr = xe - xs;
+    const uint32_t cnt = as_u32(fsub(x1r, x0r));
+    if (cnt < nfr) nfr = cnt;
+    uint32_t w0 = 0;
+    if (nfr && xs < w) {
+        o.px0 = (uint32_t)xs;
+        o.px1 = (uint32_t)(xs + nfr < w ? xs + nfr : w);
+        w0 = o.px0 | (o.px1 << 16);
+    }
+    rec[0] = w0;
+    // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102), and the
+    // varyings at the span's first tile boundary.
+    const float tshift = fsub(x0r, lx);
+    const uint32_t kb = w0 ? tile_w - (o.px0 & (tile_w - 1u)) : 0u;
+    const bool crosses = w0 && o.px0 + kb < o.px1;
+    const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
+    // The components step side by side (independent chains), each exactly
+    // like Iter::next.
+    constexpr uint32_t NCL = NCT ? (uint32_t)NCT : RF_NC;
+    float vb[NCL], dvc[NCL];
+#pragma unroll
+    for (uint32_t c = 0; c < NCL; ++c) {
+        if (c < nc) {
+            const float v = cv[c * cs];
+            dvc[c] = dvh[c];
+            vb[c] = fadd(v, fmul(fsub(fadd(v, dvc[c]), v), tshift));
+            rec[1 + c] = f2u(vb[c]);
+        } else {
+            dvc[c] = 0.0f;
+            vb[c] = 0.0f;
+        }
+    }
+    if (w0) zhi = fmaxf(zhi, span_depth_bound(vb[0], dvc[0], o.px1 - o.px0));
+    if constexpr (NCT != 0) {
+        step_k<NCT>(vb, dvc, ksteps);
+    } else {
+        switch (nc) {  // only the kind's components step
+            case 1: step_k<1>(vb, dvc, ksteps); break;
+            case 2: step_k<2>(vb, dvc, ksteps); break;
+            case 3: step_k<3>(vb, dvc, ksteps); break;
+            case 4: step_k<4>(vb, dvc, ksteps); break;
+            case 5: step_k<5>(vb, dvc, ksteps); break;
+            default: step_k<6>(vb, dvc, ksteps); break;
+        }
+    }
+#pragma unroll
+    for (uint32_t c = 0; c < NCL; ++c)
+        if (c < nc) rec[1 + nc + c] = f2u(vb[c]);
 }
 
 }  // namespace
@@ -1210,63 +1285,9 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
                         const uint32_t hh = in0 ? 0u : 1u;
                         const uint32_t i = (uint32_t)(y - bs);
                         const uint32_t ridx = in0 ? (uint32_t)(y - lo0) : inh[0] + (uint32_t)(y - lo1);
-                        const float lx = T[RF_R_LX][i], rx = T[RF_R_RX][i];
-                        const float x0r = round_up_to_half(lx), x1r = round_up_to_half(rx);
-                        const uint64_t xs = as_usize(x0r);
-                        uint64_t xe = as_usize(x1r);
-                        if (xe < xs) xe = xs;
-                        o.frags_i = xe - xs;
-                        if (xe > J.w) o.oob = 1;
-                        uint64_t nfr = xe - xs;
-                        const uint32_t cnt = as_u32(fsub(x1r, x0r));
-                        if (cnt < nfr) nfr = cnt;
-                        uint32_t w0 = 0;
-                        if (nfr && xs < J.w) {
-                            o.px0 = (uint32_t)xs;
-                            o.px1 = (uint32_t)(xs + nfr < J.w ? xs + nfr : J.w);
-                            w0 = o.px0 | (o.px1 << 16);
-                        }
-                        uint32_t *rec = rows + base + (size_t)ridx * stride;
-                        rec[0] = w0;
-                        // v0.lerp(v0.step(dv_dx), x0 - v0.x)  (raster.rs:102),
-                        // and the varyings at the span's first tile boundary.
-                        const float tshift = fsub(x0r, lx);
-                        const uint32_t kb = w0 ? tile_w - (o.px0 & (tile_w - 1u)) : 0u;
-                        const bool crosses = w0 && o.px0 + kb < o.px1;
-                        const uint32_t ksteps = crosses ? kb : 0u;  // <= tile width
-                        // The components step side by side (independent
-                        // chains), each exactly like Iter::next.
-                        const float *dvh = P->half[hh].dvdx;
-                        constexpr uint32_t NCL = NCT ? (uint32_t)NCT : RF_NC;
-                        float vb[NCL], dvc[NCL];
-#pragma unroll
-                        for (uint32_t c = 0; c < NCL; ++c) {
-                            if (c < nc) {
-                                const float cv = T[RF_R_C + c][i];
-                                dvc[c] = dvh[c];
-                                vb[c] = fadd(cv, fmul(fsub(fadd(cv, dvc[c]), cv), tshift));
-                                rec[1 + c] = f2u(vb[c]);
-                            } else {
-                                dvc[c] = 0.0f;
-                                vb[c] = 0.0f;
-                            }
-                        }
-                        if (w0) zhi_tri = fmaxf(zhi_tri, span_depth_bound(vb[0], dvc[0], o.px1 - o.px0));
-                        if constexpr (NCT != 0) {
-                            step_k<NCT>(vb, dvc, ksteps);
-                        } else {
-                            switch (nc) {  // only the kind's components step
-                                case 1: step_k<1>(vb, dvc, ksteps); break;
-                                case 2: step_k<2>(vb, dvc, ksteps); break;
-                                case 3: step_k<3>(vb, dvc, ksteps); break;
-                                case 4: step_k<4>(vb, dvc, ksteps); break;
-                                case 5: step_k<5>(vb, dvc, ksteps); break;
-                                default: step_k<6>(vb, dvc, ksteps); break;
-                            }
-                        }
-#pragma unroll
-                        for (uint32_t c = 0; c < NCL; ++c)
-                            if (c < nc) rec[1 + nc + c] = f2u(vb[c]);
+                        row_record<NCT>(T[RF_R_LX][i], T[RF_R_RX][i], &T[RF_R_C][i], RF_TILE_H + 4,
+                                        P->half[hh].dvdx, nc, J.w, tile_w, rows + base + (size_t)ridx * stride,
+                                        o, zhi_tri);
                     }
                     acc_fi += o.frags_i;
                     acc_oob += o.oob;
@@ -1333,6 +1354,203 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         wbc = wbn;
     }
     flush();
+    warp_add_u64(marks, acc_marks, true);
+}
+
+// ---------------------------------------------------------------------------
+// K3c: the same work for small triangles, eight lanes per triangle.  A
+// regular triangle with at most RF_SMALL_ROWS rows on the target (k_setup
+// puts it on the small list) would leave most of a warp idle in k_bin, so
+// here a group of eight lanes takes it -- four triangles per warp (its
+// reductions over its own lanes, the warp reconverging between phases):
+// one lane per row quantity walks the rows (both halves, ScanlineIter::next
+// in the reference's order), then one lane per row does the span, stats,
+// record and depth bound exactly as k_bin, and the group marks the (at most
+// two) bands' tiles.  A triangle whose records do not fit goes onto k_bin's
+// live list instead (k_bin runs after this kernel and takes it with the
+// rest).
+// ---------------------------------------------------------------------------
+static_assert(sizeof(RasterPrim) / 16 <= 8, "a group of eight lanes stores a RasterPrim in one pass");
+template <int NCT>
+__global__ void __launch_bounds__(256, 4)
+k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
+            const uint2 *__restrict__ live_small, uint2 *__restrict__ live, uint32_t tile_w,
+            const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
+            unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
+            StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
+            unsigned long long *__restrict__ marks) {
+    constexpr uint32_t NONE = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
+    const uint32_t g = lane >> 3, gl = lane & 7;  // group of the warp, lane in the group
+    const uint32_t gmask = 0xFFu << (8 * g);
+    const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const uint32_t ng = (gridDim.x * blockDim.x) >> 3;
+    const uint32_t tw_log2 = __ffs(tile_w) - 1;
+    const uint32_t nl = counters[RF_CNT_LIVE_SMALL];
+    __shared__ __align__(16) uint4 sbuf[8][4][RF_PRIM_CORE_BYTES / 16];  // records' first parts
+    __shared__ __align__(16) RasterPrim srp[8][4];
+    __shared__ float stab[8][4][RF_NR][RF_SMALL_ROWS];  // quantity q of row r at [q][r]
+    const PrimRec *P = reinterpret_cast<const PrimRec *>(sbuf[wib][g]);
+    RasterPrim *R = &srp[wib][g];
+    float (*T)[RF_SMALL_ROWS] = stab[wib][g];
+    uint32_t cur_job = NONE;
+    unsigned long long acc_fi = 0, acc_oob = 0;  // per lane, for cur_job
+    uint32_t acc_marks = 0;
+    auto gsum = [&](unsigned long long v) {
+        for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+        return v;
+    };
+    auto flush = [&]() {
+        if (cur_job != NONE) {
+            const unsigned long long fi = gsum(acc_fi), oob = gsum(acc_oob);
+            if (gl == 0 && fi) atomicAdd(&stats[cur_job].frags_i, fi);
+            if (gl == 0 && oob) atomicAdd(&stats[cur_job].oob, oob);
+        }
+        acc_fi = acc_oob = 0;
+    };
+    // Warp-uniform trips: the four groups of a warp take four consecutive
+    // list entries each trip, and the warp reconverges between the phases
+    // (groups left to drift apart would issue their instructions apart).
+    for (uint32_t w4 = (gid & ~3u); w4 < nl; w4 += ng) {
+        const uint32_t i = w4 + g;
+        const bool act = i < nl;
+        uint2 e = make_uint2(0u, 0u);
+        unsigned long long wb = 0;
+        if (act) {
+            e = __ldg(live_small + i);
+            wb = __ldg(tri_wbase + e.y);
+            const uint4 *src = reinterpret_cast<const uint4 *>(prims + e.x);
+            for (uint32_t q = gl; q < RF_PRIM_CORE_BYTES / 16; q += 8) sbuf[wib][g][q] = src[q];
+        }
+        __syncwarp();
+        bool run = act;
+        unsigned long long base = 0;
+        uint32_t word = 0, bit = 0, nc = 0, nr = 0, stride = 0, nrows = 0;
+        int64_t Yh[2] = {0, 0};
+        uint32_t inh[2] = {0u, 0u};
+        const JobDev *J = nullptr;
+        if (act) {
+            const uint32_t job = P->job;
+            if (job != cur_job) {
+                flush();
+                cur_job = job;
+            }
+            J = &jobs[job];
+            base = wb + P->rloc;
+            if (base + P->rwords > rows_cap) {  // no room for its records: k_bin's path
+                if (gl == 0) live[atomicAdd(&counters[RF_CNT_LIVE], 1u)] = e;
+                run = false;
+            }
+        }
+        if (run) {
+            const uint32_t tl = P->tri - J->tri_base;
+            word = tl >> 5;
+            bit = 1u << (tl & 31);
+            nc = NCT ? (uint32_t)NCT : 1 + nattr_of(P->kind);
+            nr = RF_R_C + nc;
+            stride = 1 + 2 * nc;
+            // Both halves' rows on the target (as in k_bin).
+            for (int hh = 0; hh < 2; ++hh) {
+                const HalfRec *H = &P->half[hh];
+                const uint32_t n = H->n;
+                if (n == 0) continue;
+                const float y0r = H->y0r;
+                if (!(fabsf(y0r) < RF_MAX_COORD)) {
+                    if (gl == 0) acc_oob += 1;
+                    continue;
+                }
+                const int64_t Y = (int32_t)fsub(y0r, 0.5f);
+                const int64_t in_rows = min((int64_t)n, max((int64_t)0, (int64_t)J->h - Y));
+                if (gl == 0) acc_oob += (unsigned long long)((int64_t)n - in_rows);
+                if (in_rows <= 0) continue;
+                Yh[hh] = Y;
+                inh[hh] = (uint32_t)in_rows;
+            }
+            nrows = inh[0] + inh[1];  // <= RF_SMALL_ROWS (the list's rule)
+            if (gl == 0) {
+                R->draw = P->draw;
+                R->flags = RF_RP_LIVE | RF_RP_ROWS;
+                R->kind = P->kind;
+                R->base = (uint32_t)base;
+                R->stride = stride;
+                R->y0 = (uint32_t)Yh[0];
+                R->c0 = inh[0];
+                R->y1 = (uint32_t)Yh[1];
+                R->c1 = inh[1];
+            }
+            if (gl < RF_NC) {
+                R->dvdx[0][gl] = P->half[0].dvdx[gl];
+                R->dvdx[1][gl] = P->half[1].dvdx[gl];
+            }
+            // Row quantity gl of both halves' rows, half 0's first.
+            if (gl < nr) {
+                for (int hh = 0; hh < 2; ++hh) {
+                    float v = u2f(P->half[hh].b0[gl]);
+                    const float d = P->half[hh].d[gl];
+                    const uint32_t r1 = hh ? nrows : inh[0];
+                    for (uint32_t r = hh ? inh[0] : 0u; r < r1; ++r) {
+                        T[gl][r] = v;
+                        v = fadd(v, d);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // Row gl: its span, stats, record and depth bound.
+        RowOut o{0, 0, 0xFFFFFFFFu, 0};
+        float zhi = -__int_as_float(0x7F800000);
+        uint32_t yb = NONE;  // the row's band
+        if (run && gl < nrows) {
+            const uint32_t hh = gl < inh[0] ? 0u : 1u;
+            const int64_t y = hh ? Yh[1] + (gl - inh[0]) : Yh[0] + gl;
+            yb = (uint32_t)(y / RF_TILE_H);
+            row_record<NCT>(T[RF_R_LX][gl], T[RF_R_RX][gl], &T[RF_R_C][gl], RF_SMALL_ROWS,
+                            P->half[hh].dvdx, nc, J->w, tile_w, rows + base + (size_t)gl * stride, o, zhi);
+        }
+        __syncwarp();
+        acc_fi += o.frags_i;
+        acc_oob += o.oob;
+        if (run) {
+            // The bands' tiles: the group's covered columns per band.
+            const uint32_t b_lo = __reduce_min_sync(gmask, yb);
+            const uint32_t b_hi = __reduce_max_sync(gmask, yb == NONE ? 0u : yb);
+            for (uint32_t b = b_lo; b_lo != NONE && b <= b_hi; ++b) {
+                const bool inb = yb == b && o.px0 < o.px1;
+                const uint32_t lo = __reduce_min_sync(gmask, inb ? o.px0 : NONE);
+                const uint32_t hi = __reduce_max_sync(gmask, inb ? o.px1 : 0u);
+                if (lo < hi) {
+                    const uint32_t t0 = lo >> tw_log2, t1 = (hi - 1) >> tw_log2;
+                    uint32_t *mrow = mask + J->mask_base + (size_t)b * J->tiles_x * J->mask_words + word;
+                    uint32_t *srow = mask + J->sum_base + (size_t)b * J->tiles_x * J->sum_words + (word >> 5);
+                    const uint32_t sbit = 1u << (word & 31u);
+                    for (uint32_t t = t0 + gl; t <= t1; t += 8) {
+                        atomicOr(mrow + (size_t)t * J->mask_words, bit);
+                        atomicOr(srow + (size_t)t * J->sum_words, sbit);
+                        ++acc_marks;
+                    }
+                }
+            }
+            // The triangle's depth bound: the largest of its rows'.
+            for (int o2 = 4; o2 > 0; o2 >>= 1) zhi = fmaxf(zhi, __shfl_xor_sync(gmask, zhi, o2));
+            if (gl == 0) R->zmax = zhi;
+            __syncwarp(gmask);
+            const uint4 *rs = reinterpret_cast<const uint4 *>(R);
+            uint4 *dst = reinterpret_cast<uint4 *>(rprims + e.x);
+            if (gl < sizeof(RasterPrim) / 16) dst[gl] = rs[gl];
+        }
+        __syncwarp();
+    }
+    // The stats left over, one atomic per warp when its groups ended on the
+    // same job (the usual case: a frame of one target), else per group.
+    const uint32_t has = __ballot_sync(0xFFFFFFFFu, cur_job != NONE);
+    const uint32_t j0 = has ? __shfl_sync(0xFFFFFFFFu, cur_job, __ffs(has) - 1) : NONE;
+    if (has && __all_sync(0xFFFFFFFFu, cur_job == j0 || cur_job == NONE)) {
+        warp_add_u64(&stats[j0].frags_i, acc_fi, true);
+        warp_add_u64(&stats[j0].oob, acc_oob, true);
+    } else {
+        flush();
+    }
+    __syncwarp();
     warp_add_u64(marks, acc_marks, true);
 }
 
@@ -1471,9 +1689,15 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
     uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
+    // The live list has room for every output triangle twice over: the
+    // triangles for k_bin from the start, the small ones from halfway.  (A
+    // depth-sorted frame's triangles are single clipped pieces.)
+    const size_t live_cap = perm ? (size_t)nt : (size_t)nt * RF_MAX_FAN;
+    uint2 *live_small = live + live_cap;
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
                                                 prims, tri_words, rprims, live,
-                                                counters + RF_CNT_LIVE, counters + RF_CNT_ITEMS,
+                                                counters + RF_CNT_LIVE, live_small,
+                                                counters + RF_CNT_LIVE_SMALL, counters + RF_CNT_ITEMS,
                                                 stats, perm, ptri);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -1486,17 +1710,23 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    // one warp per live output triangle; the count is only known on the device
-    uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
+    // The small triangles, eight lanes each, then one warp per other live
+    // output triangle (with the small ones that found no room for their
+    // records); the counts are only known on the device.
     auto bin = k_bin<0>;
+    auto bin_small = k_bin_small<0>;
     switch (kind) {  // components per triangle: 1 + the kind's attributes
-        case RF_K_FLAT: bin = k_bin<1>; break;
-        case RF_K_TEXTURED: bin = k_bin<3>; break;
+        case RF_K_FLAT: bin = k_bin<1>; bin_small = k_bin_small<1>; break;
+        case RF_K_TEXTURED: bin = k_bin<3>; bin_small = k_bin_small<3>; break;
         case RF_K_GOURAUD:
-        case RF_K_GOURAUD_SRGB: bin = k_bin<4>; break;
-        case RF_K_TEX_GOURAUD: bin = k_bin<6>; break;
+        case RF_K_GOURAUD_SRGB: bin = k_bin<4>; bin_small = k_bin_small<4>; break;
+        case RF_K_TEX_GOURAUD: bin = k_bin<6>; bin_small = k_bin_small<6>; break;
         default: break;
     }
+    const uint32_t sblocks = min((nt + 31) / 32, (uint32_t)nsm * 4);
+    bin_small<<<sblocks, 256, 0, s>>>(jobs, prims, live_small, live, tile_w, tri_wbase, rows, rows_cap,
+                                      rprims, mask, stats, counters, marks);
+    const uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
     bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap, rprims, mask,
                                 stats, counters, marks);
     return cudaGetLastError();
