@@ -602,7 +602,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->scan64, rfk::scan64_scratch_words((uint32_t)nt) * 8))) return st;
     if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
     if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
-    if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 16))) return st;  // two lists
+    if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 24))) return st;  // three lists
     if ((st = ensure(ctx, ctx->marks, 8))) return st;
     if ((st = ensure(ctx, ctx->items, (size_t)ntiles * (RF_SPLIT_K + 1) * 4))) return st;
     if (!ctx->rows_need_host) {

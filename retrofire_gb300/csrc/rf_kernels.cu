@@ -71,6 +71,7 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
             counters[RF_CNT_QUEUE] = 0;
             counters[RF_CNT_LIVE] = 0;
             counters[RF_CNT_LIVE_SMALL] = 0;
+            counters[RF_CNT_LIVE_MID] = 0;
             counters[RF_CNT_CLIPQ] = 0;
             *marks = 0;
         }
@@ -747,6 +748,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
                         uint2 *__restrict__ live, uint32_t *__restrict__ live_n,
                         uint2 *__restrict__ live_small, uint32_t *__restrict__ live_small_n,
+                        uint2 *__restrict__ live_mid, uint32_t *__restrict__ live_mid_n,
                         uint32_t *__restrict__ extra, StatsDev *__restrict__ stats,
                         const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ptri) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *extra = 0;  // the work list's counter
@@ -795,7 +797,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
         for (uint32_t c = 0; c < maxc; ++c) {
             const bool have = c < cnt;
             bool keep = false;  // passes the face-cull test
-            bool small = false;  // ... and goes to the small list (k_bin_small)
+            uint32_t list = 0;  // ... and its binning list: 0 k_bin, 1 / 2 k_bin_small (8 / 16 lanes)
             if (have) {
                 const DrawDev &d = draws[di];
                 const JobDev &J = jobs[job];
@@ -887,7 +889,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     P.rwords = (uint32_t)w;
                     words += (uint32_t)w;
                 }
-                small = P.rwords != 0u && rows <= RF_SMALL_ROWS;
+                if (P.rwords != 0u) list = rows <= 8u ? 1u : rows <= 16u ? 2u : 0u;
                 if (P.rwords == 0u) {  // rasterised from this record: it needs the runs
                     PrimRec *G = prims + p0 + c;
                     for (int hh = 0; hh < 2; ++hh)
@@ -899,16 +901,16 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
             const uint32_t dst = p0 + c;
             // Append this step's live triangles to their lists.
-            const uint32_t bsm = __ballot_sync(0xFFFFFFFFu, keep && small);
-            for (int which = 0; which < 2; ++which) {
-                const uint32_t b = which ? bsm : bal & ~bsm;
+            for (uint32_t which = 0; which < 3; ++which) {
+                const uint32_t b = __ballot_sync(0xFFFFFFFFu, keep && list == which);
                 if (!b) continue;
+                uint32_t *cnt_w = which == 0 ? live_n : which == 1 ? live_small_n : live_mid_n;
+                uint2 *list_w = which == 0 ? live : which == 1 ? live_small : live_mid;
                 const uint32_t lead = __ffs(b) - 1;
                 uint32_t at = 0;
-                if (lane == lead) at = atomicAdd(which ? live_small_n : live_n, (uint32_t)__popc(b));
+                if (lane == lead) at = atomicAdd(cnt_w, (uint32_t)__popc(b));
                 at = __shfl_sync(0xFFFFFFFFu, at, lead);
-                if ((b >> lane) & 1u)
-                    (which ? live_small : live)[at + __popc(b & ((1u << lane) - 1u))] = make_uint2(dst, gt);
+                if ((b >> lane) & 1u) list_w[at + __popc(b & ((1u << lane) - 1u))] = make_uint2(dst, gt);
             }
             // Write out the records built in this step, one per pass.
             while (bal) {
@@ -1358,10 +1360,10 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
 }
 
 // ---------------------------------------------------------------------------
-// K3c: the same work for small triangles, eight lanes per triangle.  A
-// regular triangle with at most RF_SMALL_ROWS rows on the target (k_setup
-// puts it on the small list) would leave most of a warp idle in k_bin, so
-// here a group of eight lanes takes it -- four triangles per warp (its
+// K3c: the same work for small triangles, G = 8 or 16 lanes per triangle.
+// A regular triangle with at most G rows on the target (k_setup puts it on
+// that group size's list) would leave most of a warp idle in k_bin, so
+// here a group of G lanes takes it -- 32 / G triangles per warp (its
 // reductions over its own lanes, the warp reconverging between phases):
 // one lane per row quantity walks the rows (both halves, ScanlineIter::next
 // in the reference's order), then one lane per row does the span, stats,
@@ -1371,33 +1373,36 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
 // rest).
 // ---------------------------------------------------------------------------
 static_assert(sizeof(RasterPrim) / 16 <= 8, "a group of eight lanes stores a RasterPrim in one pass");
-template <int NCT>
+// G: lanes per triangle (8 or 16: the list of triangles with at most G rows).
+template <int NCT, uint32_t G>
 __global__ void __launch_bounds__(256, 4)
 k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
             const uint2 *__restrict__ live_small, uint2 *__restrict__ live, uint32_t tile_w,
             const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
             unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
             StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
-            unsigned long long *__restrict__ marks) {
+            unsigned long long *__restrict__ marks, uint32_t count_slot) {
+    static_assert(G == 8 || G == 16, "group sizes");
+    constexpr uint32_t NG = 32 / G;  // groups per warp
     constexpr uint32_t NONE = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
-    const uint32_t g = lane >> 3, gl = lane & 7;  // group of the warp, lane in the group
-    const uint32_t gmask = 0xFFu << (8 * g);
-    const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-    const uint32_t ng = (gridDim.x * blockDim.x) >> 3;
+    const uint32_t g = lane / G, gl = lane & (G - 1);  // group of the warp, lane in the group
+    const uint32_t gmask = (G == 16 ? 0xFFFFu : 0xFFu) << (G * g);
+    const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const uint32_t ng = (gridDim.x * blockDim.x) / G;
     const uint32_t tw_log2 = __ffs(tile_w) - 1;
-    const uint32_t nl = counters[RF_CNT_LIVE_SMALL];
-    __shared__ __align__(16) uint4 sbuf[8][4][RF_PRIM_CORE_BYTES / 16];  // records' first parts
-    __shared__ __align__(16) RasterPrim srp[8][4];
-    __shared__ float stab[8][4][RF_NR][RF_SMALL_ROWS];  // quantity q of row r at [q][r]
+    const uint32_t nl = counters[count_slot];
+    __shared__ __align__(16) uint4 sbuf[8][NG][RF_PRIM_CORE_BYTES / 16];  // records' first parts
+    __shared__ __align__(16) RasterPrim srp[8][NG];
+    __shared__ float stab[8][NG][RF_NR][G];  // quantity q of row r at [q][r]
     const PrimRec *P = reinterpret_cast<const PrimRec *>(sbuf[wib][g]);
     RasterPrim *R = &srp[wib][g];
-    float (*T)[RF_SMALL_ROWS] = stab[wib][g];
+    float (*T)[G] = stab[wib][g];
     uint32_t cur_job = NONE;
     unsigned long long acc_fi = 0, acc_oob = 0;  // per lane, for cur_job
     uint32_t acc_marks = 0;
     auto gsum = [&](unsigned long long v) {
-        for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+        for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
         return v;
     };
     auto flush = [&]() {
@@ -1411,7 +1416,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
     // Warp-uniform trips: the four groups of a warp take four consecutive
     // list entries each trip, and the warp reconverges between the phases
     // (groups left to drift apart would issue their instructions apart).
-    for (uint32_t w4 = (gid & ~3u); w4 < nl; w4 += ng) {
+    for (uint32_t w4 = gid - g; w4 < nl; w4 += ng) {
         const uint32_t i = w4 + g;
         const bool act = i < nl;
         uint2 e = make_uint2(0u, 0u);
@@ -1420,7 +1425,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
             e = __ldg(live_small + i);
             wb = __ldg(tri_wbase + e.y);
             const uint4 *src = reinterpret_cast<const uint4 *>(prims + e.x);
-            for (uint32_t q = gl; q < RF_PRIM_CORE_BYTES / 16; q += 8) sbuf[wib][g][q] = src[q];
+            for (uint32_t q = gl; q < RF_PRIM_CORE_BYTES / 16; q += G) sbuf[wib][g][q] = src[q];
         }
         __syncwarp();
         bool run = act;
@@ -1466,7 +1471,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
                 Yh[hh] = Y;
                 inh[hh] = (uint32_t)in_rows;
             }
-            nrows = inh[0] + inh[1];  // <= RF_SMALL_ROWS (the list's rule)
+            nrows = inh[0] + inh[1];  // <= G (the list's rule)
             if (gl == 0) {
                 R->draw = P->draw;
                 R->flags = RF_RP_LIVE | RF_RP_ROWS;
@@ -1504,7 +1509,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
             const uint32_t hh = gl < inh[0] ? 0u : 1u;
             const int64_t y = hh ? Yh[1] + (gl - inh[0]) : Yh[0] + gl;
             yb = (uint32_t)(y / RF_TILE_H);
-            row_record<NCT>(T[RF_R_LX][gl], T[RF_R_RX][gl], &T[RF_R_C][gl], RF_SMALL_ROWS,
+            row_record<NCT>(T[RF_R_LX][gl], T[RF_R_RX][gl], &T[RF_R_C][gl], G,
                             P->half[hh].dvdx, nc, J->w, tile_w, rows + base + (size_t)gl * stride, o, zhi);
         }
         __syncwarp();
@@ -1523,7 +1528,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
                     uint32_t *mrow = mask + J->mask_base + (size_t)b * J->tiles_x * J->mask_words + word;
                     uint32_t *srow = mask + J->sum_base + (size_t)b * J->tiles_x * J->sum_words + (word >> 5);
                     const uint32_t sbit = 1u << (word & 31u);
-                    for (uint32_t t = t0 + gl; t <= t1; t += 8) {
+                    for (uint32_t t = t0 + gl; t <= t1; t += G) {
                         atomicOr(mrow + (size_t)t * J->mask_words, bit);
                         atomicOr(srow + (size_t)t * J->sum_words, sbit);
                         ++acc_marks;
@@ -1531,7 +1536,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
                 }
             }
             // The triangle's depth bound: the largest of its rows'.
-            for (int o2 = 4; o2 > 0; o2 >>= 1) zhi = fmaxf(zhi, __shfl_xor_sync(gmask, zhi, o2));
+            for (int o2 = G / 2; o2 > 0; o2 >>= 1) zhi = fmaxf(zhi, __shfl_xor_sync(gmask, zhi, o2));
             if (gl == 0) R->zmax = zhi;
             __syncwarp(gmask);
             const uint4 *rs = reinterpret_cast<const uint4 *>(R);
@@ -1689,15 +1694,17 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
     uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
-    // The live list has room for every output triangle twice over: the
-    // triangles for k_bin from the start, the small ones from halfway.  (A
+    // The live list has room for every output triangle three times over:
+    // the triangles for k_bin from the start, those with at most 8 rows from
+    // a third of the way, those with 9 to 16 rows from two thirds.  (A
     // depth-sorted frame's triangles are single clipped pieces.)
     const size_t live_cap = perm ? (size_t)nt : (size_t)nt * RF_MAX_FAN;
-    uint2 *live_small = live + live_cap;
+    uint2 *live_small = live + live_cap, *live_mid = live + 2 * live_cap;
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
                                                 prims, tri_words, rprims, live,
                                                 counters + RF_CNT_LIVE, live_small,
-                                                counters + RF_CNT_LIVE_SMALL, counters + RF_CNT_ITEMS,
+                                                counters + RF_CNT_LIVE_SMALL, live_mid,
+                                                counters + RF_CNT_LIVE_MID, counters + RF_CNT_ITEMS,
                                                 stats, perm, ptri);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -1714,18 +1721,21 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     // output triangle (with the small ones that found no room for their
     // records); the counts are only known on the device.
     auto bin = k_bin<0>;
-    auto bin_small = k_bin_small<0>;
+    auto bin8 = k_bin_small<0, 8>;
+    auto bin16 = k_bin_small<0, 16>;
     switch (kind) {  // components per triangle: 1 + the kind's attributes
-        case RF_K_FLAT: bin = k_bin<1>; bin_small = k_bin_small<1>; break;
-        case RF_K_TEXTURED: bin = k_bin<3>; bin_small = k_bin_small<3>; break;
+        case RF_K_FLAT: bin = k_bin<1>; bin8 = k_bin_small<1, 8>; bin16 = k_bin_small<1, 16>; break;
+        case RF_K_TEXTURED: bin = k_bin<3>; bin8 = k_bin_small<3, 8>; bin16 = k_bin_small<3, 16>; break;
         case RF_K_GOURAUD:
-        case RF_K_GOURAUD_SRGB: bin = k_bin<4>; bin_small = k_bin_small<4>; break;
-        case RF_K_TEX_GOURAUD: bin = k_bin<6>; bin_small = k_bin_small<6>; break;
+        case RF_K_GOURAUD_SRGB: bin = k_bin<4>; bin8 = k_bin_small<4, 8>; bin16 = k_bin_small<4, 16>; break;
+        case RF_K_TEX_GOURAUD: bin = k_bin<6>; bin8 = k_bin_small<6, 8>; bin16 = k_bin_small<6, 16>; break;
         default: break;
     }
     const uint32_t sblocks = min((nt + 31) / 32, (uint32_t)nsm * 4);
-    bin_small<<<sblocks, 256, 0, s>>>(jobs, prims, live_small, live, tile_w, tri_wbase, rows, rows_cap,
-                                      rprims, mask, stats, counters, marks);
+    bin8<<<sblocks, 256, 0, s>>>(jobs, prims, live_small, live, tile_w, tri_wbase, rows, rows_cap, rprims,
+                                 mask, stats, counters, marks, RF_CNT_LIVE_SMALL);
+    bin16<<<sblocks, 256, 0, s>>>(jobs, prims, live_mid, live, tile_w, tri_wbase, rows, rows_cap, rprims,
+                                  mask, stats, counters, marks, RF_CNT_LIVE_MID);
     const uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
     bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap, rprims, mask,
                                 stats, counters, marks);

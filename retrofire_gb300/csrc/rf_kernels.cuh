@@ -48,8 +48,8 @@
 #define RF_CNT_LIVE 7     // output triangles that passed the face-cull test
 #define RF_CNT_ITEMS 8    // rasteriser work items after the first ntiles (slices of crowded tiles)
 #define RF_CNT_CLIPQ 10   // triangles queued for clipping
-#define RF_CNT_LIVE_SMALL 11  // live triangles binned eight lanes each (at most RF_SMALL_ROWS rows)
-#define RF_SMALL_ROWS 8u
+#define RF_CNT_LIVE_SMALL 11  // live triangles binned eight lanes each (at most 8 rows)
+#define RF_CNT_LIVE_MID 12    // live triangles binned sixteen lanes each (9 to 16 rows)
 #define RF_CNT_N 16
 #define RF_SCAN_BLOCK_ITEMS 4096u  // values one scan block takes (one launch instead of three)
 
@@ -78,11 +78,12 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 // statistics, row records and tile binning (k_bin).  tri_words (nt u32), tri_wbase (nt
 // u64) and scan64 (scan64_scratch_words(nt) u64) are scratch; rows holds
 // rows_cap words; rows_total receives the words the frame asked for; live
-// (room for twice every output triangle) receives, for each triangle that
-// passes the face-cull test, its index and its input triangle's (the
-// record's tri): the small ones (regular, at most RF_SMALL_ROWS rows on the
-// target, counters[RF_CNT_LIVE_SMALL]) in its second half, the rest
-// (counters[RF_CNT_LIVE]) in its first; *marks
+// (room for three times every output triangle) receives, for each triangle
+// that passes the face-cull test, its index and its input triangle's (the
+// record's tri): the regular ones with at most 8 rows on the target
+// (counters[RF_CNT_LIVE_SMALL]) in its second third, with 9 to 16 rows
+// (counters[RF_CNT_LIVE_MID]) in its last, the rest (counters[RF_CNT_LIVE])
+// in its first; *marks
 // receives the (triangle, tile) bits set in all.  kind: the shader kind of
 // every draw, or RF_K_ANY (the binning kernel is specialised for the first).
 size_t scan64_scratch_words(uint32_t n);

@@ -65,7 +65,7 @@ constexpr size_t OFF_ROWTOT = al(OFF_SCAN64 + 64 * 8);
 constexpr size_t OFF_RPRIMS = al(OFF_ROWTOT + 8);
 constexpr size_t OFF_LIVE =
     al(OFF_RPRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(RasterPrim));
-constexpr size_t OFF_MARKS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 16);
+constexpr size_t OFF_MARKS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 24);
 constexpr size_t OFF_ITEMS = al(OFF_MARKS + 16);
 constexpr size_t OFF_ROWS = al(OFF_ITEMS + (size_t)MAX_TILES * (RF_SPLIT_K + 1) * 4);
 // The rest of the area holds row records; triangles whose records do not
