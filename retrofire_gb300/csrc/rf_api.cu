@@ -856,8 +856,9 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         tuned->pending = true;
     }
     // vertex, clip (2), scan (3, or 1 for one block), setup, scan64 (the same),
-    // bin, work list, raster (+ the stats fold)
-    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 9 : 13) + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
+    // bin (3: 8- and 16-lane groups, then warps), work list, raster (+ the
+    // stats fold)
+    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 11 : 15) + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -906,6 +907,7 @@ rf_status upload_mesh(rf_ctx *ctx, const float *verts, uint32_t nverts, uint32_t
     if (e == cudaSuccess && vb) e = cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && ib) e = cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = rfk::launch_mesh_bbox(m.verts, nverts, pos_dim + nattr, m.bbox, ctx->stream);
+    ctx->kernels += 2;
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         cudaFree(m.verts);
@@ -1252,7 +1254,10 @@ rf_status rf_mesh_update(rf_ctx *ctx, rf_mesh mesh, const float *verts, const ui
     if (st) return st;
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->stream));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->stream));
-    if (verts) CK(rfk::launch_mesh_bbox(m.verts, m.nverts, m.pos_dim + m.nattr, m.bbox, ctx->stream));
+    if (verts) {
+        CK(rfk::launch_mesh_bbox(m.verts, m.nverts, m.pos_dim + m.nattr, m.bbox, ctx->stream));
+        ctx->kernels += 2;
+    }
     CK(cudaStreamSynchronize(ctx->stream));
     return RF_OK;
 }
@@ -1272,7 +1277,10 @@ rf_status rf_mesh_update_async(rf_ctx *ctx, rf_mesh mesh, const float *verts, co
     CK(cudaStreamWaitEvent(ctx->up, m.used, 0));
     if (verts && vb) CK(cudaMemcpyAsync(m.verts, verts, vb, cudaMemcpyHostToDevice, ctx->up));
     if (idx && ib) CK(cudaMemcpyAsync(m.idx, idx, ib, cudaMemcpyHostToDevice, ctx->up));
-    if (verts) CK(rfk::launch_mesh_bbox(m.verts, m.nverts, m.pos_dim + m.nattr, m.bbox, ctx->up));
+    if (verts) {
+        CK(rfk::launch_mesh_bbox(m.verts, m.nverts, m.pos_dim + m.nattr, m.bbox, ctx->up));
+        ctx->kernels += 2;
+    }
     CK(cudaEventRecord(m.ready, ctx->up));
     m.ready_pending = true;
     return RF_OK;

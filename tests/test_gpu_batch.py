@@ -231,7 +231,9 @@ def test_graph_replay_same_shape():
         cnt = dev.counts()
         assert cnt["graphs_cached"] == 1
         assert cnt["graph_launches"] == 6
-        assert cnt["kernels"] == 6 * 9  # nine kernels per frame (one-block scans)
+        # per frame: eleven render kernels (one-block scans) and the mesh
+        # upload's two bounding-box kernels
+        assert cnt["kernels"] == 6 * (11 + 2)
     finally:
         dev.close()
 
