@@ -124,7 +124,7 @@ struct rf_ctx {
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
-    DevBuf triw, trib, scan64, rowtot, rows, rprims, live, marks, items, jstats;
+    DevBuf rowtot, rows, rprims, live, marks, items, jstats;
     DevBuf lrec, lmask;  // line pass
     // depth-sorted frames: sorted order, source triangles, per-draw counts,
     // sort scratch, the setup pass's draws / jobs, the raster's unit arrays
@@ -597,9 +597,6 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->prims, (size_t)nt * RF_MAX_FAN * sizeof(PrimRec)))) return st;
     if ((st = ensure(ctx, ctx->mask, mask_words * 4))) return st;
     if ((st = ensure(ctx, ctx->scan, rfk::scan_scratch_words((uint32_t)nt) * 4))) return st;
-    if ((st = ensure(ctx, ctx->triw, nt * 4))) return st;
-    if ((st = ensure(ctx, ctx->trib, nt * 8))) return st;
-    if ((st = ensure(ctx, ctx->scan64, rfk::scan64_scratch_words((uint32_t)nt) * 8))) return st;
     if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
     if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
     if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 24))) return st;  // three lists
@@ -682,8 +679,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(mark(RF_STAGE_SETUP));
         CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
                              P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
-                             P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
-                             P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
+                             P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
                              P<uint32_t>(ctx->mask), P<uint2>(ctx->live), P<unsigned long long>(ctx->marks),
                              kst, counters, ctx->nsm, s, nullptr, nullptr, kind));
@@ -766,9 +762,6 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         if ((st2 = ensure(ctx, ctx->scan,
                           rfk::scan_scratch_words(std::max<uint32_t>(rfk::dsort_scan_items(n32), (uint32_t)nt)) * 4)))
             return st2;
-        if ((st2 = ensure(ctx, ctx->triw, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
-        if ((st2 = ensure(ctx, ctx->trib, (size_t)std::max<uint32_t>(n32, 1) * 8))) return st2;
-        if ((st2 = ensure(ctx, ctx->scan64, rfk::scan64_scratch_words(n32) * 8))) return st2;
         if ((st2 = ensure(ctx, ctx->vtoff, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
         if ((st2 = ensure(ctx, ctx->vtcnt, (size_t)std::max<uint32_t>(n32, 1) * 4))) return st2;
         if ((st2 = ensure(ctx, ctx->vdraws, vd.size() * sizeof(DrawDev)))) return st2;
@@ -786,8 +779,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(rfk::launch_iota(P<uint32_t>(ctx->vtoff), P<uint32_t>(ctx->vtcnt), n32, s));
         CK(rfk::launch_setup(vdd, ndraws, vjd, n32, TW, P<float4>(ctx->cpos), P<uint32_t>(ctx->tcnt),
                              P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
-                             P<PrimRec>(ctx->prims), P<uint32_t>(ctx->triw), P<unsigned long long>(ctx->trib),
-                             P<unsigned long long>(ctx->scan64), P<unsigned long long>(ctx->rowtot),
+                             P<PrimRec>(ctx->prims), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
                              P<uint32_t>(ctx->mask), P<uint2>(ctx->live), P<unsigned long long>(ctx->marks),
                              kst, counters, ctx->nsm, s, P<uint32_t>(ctx->perm), P<uint32_t>(ctx->ptri), kind));
@@ -855,10 +847,9 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(cudaEventRecord(tuned->e1, s));
         tuned->pending = true;
     }
-    // vertex, clip (2), scan (3, or 1 for one block), setup, scan64 (the same),
-    // bin (3: 8- and 16-lane groups, then warps), work list, raster (+ the
-    // stats fold)
-    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 11 : 15) + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
+    // vertex, clip (2), scan (3, or 1 for one block), setup, bin (3: 8- and
+    // 16-lane groups, then warps), work list, raster (+ the stats fold)
+    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 10 : 12) + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -1054,7 +1045,7 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     }
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
-                      &ctx->counters, &ctx->stats, &ctx->triw, &ctx->trib, &ctx->scan64,
+                      &ctx->counters, &ctx->stats,
                       &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->marks, &ctx->items, &ctx->jstats, &ctx->lrec, &ctx->lmask,
                       &ctx->perm, &ctx->ptri, &ctx->nout, &ctx->dsort, &ctx->vdraws, &ctx->vjobs,
                       &ctx->vtoff, &ctx->vtcnt};

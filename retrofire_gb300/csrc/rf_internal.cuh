@@ -109,7 +109,7 @@ struct PrimRec {
     uint32_t live;    // 1: passed the face-cull test (only those get a record)
     uint32_t tri;     // global input triangle it was clipped from
     int32_t kind;     // shader kind of its draw
-    uint32_t rloc;    // word offset of its row records inside its input triangle's block
+    uint32_t rloc;    // word offset of its row records in the frame's row buffer
     uint32_t rwords;  // words of row records; 0 = rasterised from this record instead
     uint32_t job;     // scene (job) of its draw
     uint32_t pad_;

@@ -579,95 +579,6 @@ __global__ void k_scan_add(uint32_t *__restrict__ out, uint32_t n, const uint32_
         if (base + i < n) out[base + i] += add;
 }
 
-// Exclusive scan of u32 values into u64 (row-record offsets).
-__global__ void k_scan64_blocks(const uint32_t *__restrict__ in, unsigned long long *__restrict__ out,
-                                uint32_t n, unsigned long long *__restrict__ block_sums,
-                                unsigned long long *__restrict__ total) {
-    __shared__ unsigned long long warp_sums[32];
-    const uint32_t base = blockIdx.x * (SCAN_THREADS * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
-    unsigned long long v[SCAN_ITEMS], s = 0;
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-        v[i] = base + i < n ? in[base + i] : 0u;
-        s += v[i];
-    }
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned long long incl = s;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
-    }
-    if (lane == 31) warp_sums[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-        unsigned long long ws = warp_sums[lane], wi = ws;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-            if (lane >= (uint32_t)o) wi += y;
-        }
-        warp_sums[lane] = wi - ws;
-        if (lane == 31) {
-            block_sums[blockIdx.x] = wi;
-            if (gridDim.x == 1) *total = wi;
-        }
-    }
-    __syncthreads();
-    unsigned long long run = warp_sums[wid] + incl - s;
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i) {
-        if (base + i < n) out[base + i] = run;
-        run += v[i];
-    }
-}
-
-__global__ void k_scan64_sums(unsigned long long *__restrict__ sums, uint32_t nb,
-                              unsigned long long *__restrict__ total) {
-    __shared__ unsigned long long warp_sums[32];
-    __shared__ unsigned long long carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (uint32_t base = 0; base < nb; base += blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        const unsigned long long s = i < nb ? sums[i] : 0u;
-        unsigned long long incl = s;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += y;
-        }
-        if (lane == 31) warp_sums[wid] = incl;
-        __syncthreads();
-        if (wid == 0) {
-            unsigned long long ws = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0u, wi = ws;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-                if (lane >= (uint32_t)o) wi += y;
-            }
-            warp_sums[lane] = wi - ws;
-        }
-        __syncthreads();
-        const unsigned long long excl = carry + warp_sums[wid] + incl - s;
-        if (i < nb) sums[i] = excl;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = excl + s;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total = carry;
-}
-
-__global__ void k_scan64_add(unsigned long long *__restrict__ out, uint32_t n,
-                             const unsigned long long *__restrict__ sums) {
-    const uint32_t base = blockIdx.x * (SCAN_THREADS * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
-    const unsigned long long add = sums[blockIdx.x];
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; ++i)
-        if (base + i < n) out[base + i] += add;
-}
-
 // ---------------------------------------------------------------------------
 // K3: triangle setup.
 // ---------------------------------------------------------------------------
@@ -745,7 +656,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const float4 *__restrict__ cpos, const uint32_t *__restrict__ tcnt,
                         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ tpoly,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
-                        uint32_t *__restrict__ tri_words, RasterPrim *__restrict__ rprims,
+                        unsigned long long *__restrict__ rows_total, RasterPrim *__restrict__ rprims,
                         uint2 *__restrict__ live, uint32_t *__restrict__ live_n,
                         uint2 *__restrict__ live_small, uint32_t *__restrict__ live_small_n,
                         uint2 *__restrict__ live_mid, uint32_t *__restrict__ live_mid_n,
@@ -793,7 +704,6 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
             }
         }
         const uint32_t maxc = __reduce_max_sync(0xFFFFFFFFu, cnt);
-        uint32_t words = 0;  // row-record words of this input triangle so far
         for (uint32_t c = 0; c < maxc; ++c) {
             const bool have = c < cnt;
             bool keep = false;  // passes the face-cull test
@@ -852,7 +762,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 P.live = 1u;
                 P.tri = gt;
                 P.kind = d.shader;
-                P.rloc = words;
+                P.rloc = 0;
                 P.rwords = 0;
                 P.job = job;
                 prims_o += 1;
@@ -885,10 +795,7 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                     rows += (uint32_t)in;
                 }
                 const uint64_t w = regular ? (uint64_t)rows * (1u + 2u * nc) : 0u;
-                if (w < 0x40000000ull && (uint64_t)words + w < 0x40000000ull) {
-                    P.rwords = (uint32_t)w;
-                    words += (uint32_t)w;
-                }
+                if (w < 0x40000000ull) P.rwords = (uint32_t)w;
                 if (P.rwords != 0u) list = rows <= 8u ? 1u : rows <= 16u ? 2u : 0u;
                 if (P.rwords == 0u) {  // rasterised from this record: it needs the runs
                     PrimRec *G = prims + p0 + c;
@@ -896,6 +803,27 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         for (uint32_t r = 0; r < RF_NR; ++r) half_runs(P.half[hh], G->runs[hh], r);
                 }
                 }
+            }
+            __syncwarp();
+            // Room for this step's row records: one atomic per warp on the
+            // frame's running total, each lane's block after the lower
+            // lanes' (the records' place in the buffer is free; each
+            // triangle's own records stay contiguous).  An offset past 32
+            // bits is clamped, so the binning pass finds no room for it.
+            {
+                PrimRec &P = *reinterpret_cast<PrimRec *>(sbuf[threadIdx.x]);
+                const unsigned long long w = keep ? P.rwords : 0u;
+                unsigned long long incl = w;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= (uint32_t)o) incl += y;
+                }
+                const unsigned long long total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                unsigned long long at = 0;
+                if (total && lane == 0) at = atomicAdd(rows_total, total);
+                at = __shfl_sync(0xFFFFFFFFu, at, 0) + (incl - w);
+                if (w) P.rloc = at < 0xFFFFFFFFull ? (uint32_t)at : 0xFFFFFFFFu;
             }
             __syncwarp();
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
@@ -923,7 +851,6 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
             }
             __syncwarp();
         }
-        if (active) tri_words[gt] = words;
         // Stats, aggregated per warp when all lanes share one job.
         const uint32_t hasjob = __ballot_sync(0xFFFFFFFFu, job != 0xFFFFFFFFu);
         if (hasjob) {
@@ -1081,9 +1008,8 @@ template <int NCT>
 __global__ void __launch_bounds__(256, 4)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
       PrimRec *__restrict__ prims, const uint2 *__restrict__ live, uint32_t tile_w,
-      const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
-      unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
-      StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
+      uint32_t *__restrict__ rows, unsigned long long rows_cap, RasterPrim *__restrict__ rprims,
+      uint32_t *__restrict__ mask, StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
       unsigned long long *__restrict__ marks) {
     const uint32_t lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1116,9 +1042,6 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     // (live entry: the output triangle's index, its input triangle's)
     uint2 pc = wid < nl ? __ldg(live + wid) : make_uint2(0u, 0u);
     uint2 pn = wid + nw < nl ? __ldg(live + wid + nw) : make_uint2(0u, 0u);
-    // The current triangle's first row-record word (of its input triangle);
-    // the next one's is loaded an iteration ahead.
-    unsigned long long wbc = wid < nl ? __ldg(tri_wbase + pc.y) : 0ull;
     fetch(sbuf[wib][0], pc.x, wid < nl);
     RasterPrim *R = &srp[wib];
     float (*T)[RF_TILE_H + 4] = stab[wib];
@@ -1153,7 +1076,6 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     };
     for (uint32_t i = wid; i < nl; i += nw) {
         const uint2 pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : make_uint2(0u, 0u);
-        const unsigned long long wbn = i + nw < nl ? __ldg(tri_wbase + pn.y) : 0ull;
         __syncwarp();  // the other slot's previous triangle is done
         fetch(sbuf[wib][cur ^ 1u], pn.x, i + nw < nl);
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
@@ -1189,7 +1111,7 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             bool regular = P->rwords != 0;
             unsigned long long base = 0;
             if (regular) {
-                base = wbc + P->rloc;
+                base = P->rloc;
                 if (base + P->rwords > rows_cap) {  // no room: rasterise from the PrimRec
                     regular = false;
                     if (lane == 0) atomicAdd(&counters[RF_CNT_ROWSOVF], 1u);
@@ -1353,7 +1275,6 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
             uint4 *dst = reinterpret_cast<uint4 *>(rprims + p);
             if (lane < sizeof(RasterPrim) / 16) dst[lane] = src[lane];
         }
-        wbc = wbn;
     }
     flush();
     warp_add_u64(marks, acc_marks, true);
@@ -1378,8 +1299,7 @@ template <int NCT, uint32_t G>
 __global__ void __launch_bounds__(256, 4)
 k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
             const uint2 *__restrict__ live_small, uint2 *__restrict__ live, uint32_t tile_w,
-            const unsigned long long *__restrict__ tri_wbase, uint32_t *__restrict__ rows,
-            unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
+            uint32_t *__restrict__ rows, unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
             StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
             unsigned long long *__restrict__ marks, uint32_t count_slot) {
     static_assert(G == 8 || G == 16, "group sizes");
@@ -1420,10 +1340,8 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
         const uint32_t i = w4 + g;
         const bool act = i < nl;
         uint2 e = make_uint2(0u, 0u);
-        unsigned long long wb = 0;
         if (act) {
             e = __ldg(live_small + i);
-            wb = __ldg(tri_wbase + e.y);
             const uint4 *src = reinterpret_cast<const uint4 *>(prims + e.x);
             for (uint32_t q = gl; q < RF_PRIM_CORE_BYTES / 16; q += G) sbuf[wib][g][q] = src[q];
         }
@@ -1441,7 +1359,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
                 cur_job = job;
             }
             J = &jobs[job];
-            base = wb + P->rloc;
+            base = P->rloc;
             if (base + P->rwords > rows_cap) {  // no room for its records: k_bin's path
                 if (gl == 0) live[atomicAdd(&counters[RF_CNT_LIVE], 1u)] = e;
                 run = false;
@@ -1677,20 +1595,16 @@ cudaError_t launch_mesh_bbox(const float *verts, uint32_t nverts, uint32_t strid
     return cudaGetLastError();
 }
 
-size_t scan64_scratch_words(uint32_t n) {
-    return (n + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS) + 1;
-}
-
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, uint32_t *tri_words,
-                         unsigned long long *tri_wbase, unsigned long long *scan64,
-                         unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
+                         PrimRec *prims, unsigned long long *rows_total, uint32_t *rows,
+                         unsigned long long rows_cap,
                          RasterPrim *rprims, uint32_t *mask, uint2 *live, unsigned long long *marks,
                          StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
                          const uint32_t *perm, const uint32_t *ptri, int kind) {
-    cudaError_t e;
+    cudaError_t e = cudaMemsetAsync(rows_total, 0, 8, s);  // the frame's row-record words
+    if (e != cudaSuccess) return e;
     if (nt == 0)  // no setup pass to zero the work-list counter
         return cudaMemsetAsync(counters + RF_CNT_ITEMS, 0, 4, s);
     uint32_t blocks = min((nt + RF_SETUP_THREADS - 1) / RF_SETUP_THREADS, (uint32_t)nsm * 32);
@@ -1701,20 +1615,11 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     const size_t live_cap = perm ? (size_t)nt : (size_t)nt * RF_MAX_FAN;
     uint2 *live_small = live + live_cap, *live_mid = live + 2 * live_cap;
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
-                                                prims, tri_words, rprims, live,
+                                                prims, rows_total, rprims, live,
                                                 counters + RF_CNT_LIVE, live_small,
                                                 counters + RF_CNT_LIVE_SMALL, live_mid,
                                                 counters + RF_CNT_LIVE_MID, counters + RF_CNT_ITEMS,
                                                 stats, perm, ptri);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    // Row-record offsets of the input triangles (64-bit: the total may not fit 32).
-    const uint32_t nb = (nt + SCAN_THREADS * SCAN_ITEMS - 1) / (SCAN_THREADS * SCAN_ITEMS);
-    k_scan64_blocks<<<nb, SCAN_THREADS, 0, s>>>(tri_words, tri_wbase, nt, scan64, rows_total);
-    if (nb > 1) {
-        k_scan64_sums<<<1, 1024, 0, s>>>(scan64, nb, rows_total);
-        k_scan64_add<<<nb, SCAN_THREADS, 0, s>>>(tri_wbase, nt, scan64);
-    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // The small triangles, eight lanes each, then one warp per other live
@@ -1732,13 +1637,13 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
         default: break;
     }
     const uint32_t sblocks = min((nt + 31) / 32, (uint32_t)nsm * 4);
-    bin8<<<sblocks, 256, 0, s>>>(jobs, prims, live_small, live, tile_w, tri_wbase, rows, rows_cap, rprims,
-                                 mask, stats, counters, marks, RF_CNT_LIVE_SMALL);
-    bin16<<<sblocks, 256, 0, s>>>(jobs, prims, live_mid, live, tile_w, tri_wbase, rows, rows_cap, rprims,
-                                  mask, stats, counters, marks, RF_CNT_LIVE_MID);
+    bin8<<<sblocks, 256, 0, s>>>(jobs, prims, live_small, live, tile_w, rows, rows_cap, rprims, mask, stats,
+                                 counters, marks, RF_CNT_LIVE_SMALL);
+    bin16<<<sblocks, 256, 0, s>>>(jobs, prims, live_mid, live, tile_w, rows, rows_cap, rprims, mask, stats,
+                                  counters, marks, RF_CNT_LIVE_MID);
     const uint32_t wblocks = min((nt * 2 + 7) / 8, (uint32_t)nsm * 16);
-    bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, tri_wbase, rows, rows_cap, rprims, mask,
-                                stats, counters, marks);
+    bin<<<wblocks, 256, 0, s>>>(draws, jobs, prims, live, tile_w, rows, rows_cap, rprims, mask, stats,
+                                counters, marks);
     return cudaGetLastError();
 }
 

@@ -74,28 +74,25 @@ cudaError_t launch_mesh_bbox(const float *verts, uint32_t nverts, uint32_t strid
 size_t scan_scratch_words(uint32_t n);
 cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch,
                         uint32_t *total, cudaStream_t s);
-// Triangle setup (k_setup), the scan of row-record sizes, then scanline
-// statistics, row records and tile binning (k_bin).  tri_words (nt u32), tri_wbase (nt
-// u64) and scan64 (scan64_scratch_words(nt) u64) are scratch; rows holds
-// rows_cap words; rows_total receives the words the frame asked for; live
-// (room for three times every output triangle) receives, for each triangle
-// that passes the face-cull test, its index and its input triangle's (the
-// record's tri): the regular ones with at most 8 rows on the target
-// (counters[RF_CNT_LIVE_SMALL]) in its second third, with 9 to 16 rows
-// (counters[RF_CNT_LIVE_MID]) in its last, the rest (counters[RF_CNT_LIVE])
-// in its first; *marks
-// receives the (triangle, tile) bits set in all.  kind: the shader kind of
-// every draw, or RF_K_ANY (the binning kernel is specialised for the first).
-size_t scan64_scratch_words(uint32_t n);
+// Triangle setup (k_setup), then scanline statistics, row records and tile
+// binning (k_bin_small for triangles of at most 8 and of 9 to 16 rows,
+// then k_bin).  rows holds rows_cap words; rows_total (zeroed here)
+// receives the words the frame asked for, each triangle's records placed
+// by k_setup from it; live (room for three times every output triangle)
+// receives, for each triangle that passes the face-cull test, its index
+// and its input triangle's (the record's tri): the regular ones with at
+// most 8 rows on the target (counters[RF_CNT_LIVE_SMALL]) in its second
+// third, with 9 to 16 rows (counters[RF_CNT_LIVE_MID]) in its last, the
+// rest (counters[RF_CNT_LIVE]) in its first; *marks receives the
+// (triangle, tile) bits set in all.  kind: the shader kind of every draw,
+// or RF_K_ANY (the binning kernels are specialised for the first).
 cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, uint32_t nt,
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
-                         PrimRec *prims, uint32_t *tri_words,
-                         unsigned long long *tri_wbase, unsigned long long *scan64,
-                         unsigned long long *rows_total, uint32_t *rows, unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint2 *live, unsigned long long *marks,
-                         StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
-                         const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr,
+                         PrimRec *prims, unsigned long long *rows_total, uint32_t *rows,
+                         unsigned long long rows_cap, RasterPrim *rprims, uint32_t *mask, uint2 *live,
+                         unsigned long long *marks, StatsDev *stats, uint32_t *counters, int nsm,
+                         cudaStream_t s, const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr,
                          int kind = RF_K_ANY);
 // The rasteriser's work list from the tile masks and the marks total
 // (slots: the warps the rasteriser keeps resident, about).  items (room

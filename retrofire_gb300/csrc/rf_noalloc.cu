@@ -58,10 +58,7 @@ constexpr size_t OFF_POOL = al(OFF_SCAN + 64 * 4);
 constexpr size_t OFF_PRIMS =
     al(OFF_POOL + (size_t)RF_NOALLOC_MAX_TRIS * RF_POLY_STORE * sizeof(PolyVert));
 constexpr size_t OFF_MASK = al(OFF_PRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(PrimRec));
-constexpr size_t OFF_TRIW = al(OFF_MASK + (size_t)MAX_TILES * (MASK_WORDS + SUM_WORDS) * 4);
-constexpr size_t OFF_TRIB = al(OFF_TRIW + (size_t)RF_NOALLOC_MAX_TRIS * 4);
-constexpr size_t OFF_SCAN64 = al(OFF_TRIB + (size_t)RF_NOALLOC_MAX_TRIS * 8);
-constexpr size_t OFF_ROWTOT = al(OFF_SCAN64 + 64 * 8);
+constexpr size_t OFF_ROWTOT = al(OFF_MASK + (size_t)MAX_TILES * (MASK_WORDS + SUM_WORDS) * 4);
 constexpr size_t OFF_RPRIMS = al(OFF_ROWTOT + 8);
 constexpr size_t OFF_LIVE =
     al(OFF_RPRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(RasterPrim));
@@ -234,9 +231,6 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     PolyVert *pool = reinterpret_cast<PolyVert *>(base + OFF_POOL);
     PrimRec *prims = reinterpret_cast<PrimRec *>(base + OFF_PRIMS);
     uint32_t *mask = reinterpret_cast<uint32_t *>(base + OFF_MASK);
-    uint32_t *triw = reinterpret_cast<uint32_t *>(base + OFF_TRIW);
-    unsigned long long *trib = reinterpret_cast<unsigned long long *>(base + OFF_TRIB);
-    unsigned long long *scan64 = reinterpret_cast<unsigned long long *>(base + OFF_SCAN64);
     unsigned long long *rowtot = reinterpret_cast<unsigned long long *>(base + OFF_ROWTOT);
     RasterPrim *rprims = reinterpret_cast<RasterPrim *>(base + OFF_RPRIMS);
     uint2 *live = reinterpret_cast<uint2 *>(base + OFF_LIVE);
@@ -260,7 +254,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
                                cnt, nsm, s));
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
-                                triw, trib, scan64, rowtot, rows, ROWS_WORDS, rprims, mask, live,
+                                rowtot, rows, ROWS_WORDS, rprims, mask, live,
                                 marks, sd, cnt, nsm, s, nullptr, nullptr, shader));
         NA_CK(rfk::launch_items(jd, 1, mask, ntiles, marks, (uint32_t)nsm * 16u, items, cnt, s));
         const bool fast = depth && flags->depth_test == RF_DEPTH_LESS && flags->color_write &&
