@@ -599,7 +599,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->scan, rfk::scan_scratch_words((uint32_t)nt) * 4))) return st;
     if ((st = ensure(ctx, ctx->rowtot, 8))) return st;
     if ((st = ensure(ctx, ctx->rprims, (size_t)nt * RF_MAX_FAN * sizeof(RasterPrim)))) return st;
-    if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 24))) return st;  // three lists
+    if ((st = ensure(ctx, ctx->live, (size_t)nt * RF_MAX_FAN * 12))) return st;  // three lists
     if ((st = ensure(ctx, ctx->marks, 8))) return st;
     if ((st = ensure(ctx, ctx->items, (size_t)ntiles * (RF_SPLIT_K + 1) * 4))) return st;
     if (!ctx->rows_need_host) {
@@ -681,7 +681,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                              P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
                              P<PolyVert>(ctx->pool), P<PrimRec>(ctx->prims), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
-                             P<uint32_t>(ctx->mask), P<uint2>(ctx->live), P<unsigned long long>(ctx->marks),
+                             P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
                              kst, counters, ctx->nsm, s, nullptr, nullptr, kind));
         CK(rfk::launch_items(jd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
                              (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));
@@ -781,7 +781,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                              P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly), P<PolyVert>(ctx->pool),
                              P<PrimRec>(ctx->prims), P<unsigned long long>(ctx->rowtot),
                              P<uint32_t>(ctx->rows), ctx->rows_cap, P<RasterPrim>(ctx->rprims),
-                             P<uint32_t>(ctx->mask), P<uint2>(ctx->live), P<unsigned long long>(ctx->marks),
+                             P<uint32_t>(ctx->mask), P<uint32_t>(ctx->live), P<unsigned long long>(ctx->marks),
                              kst, counters, ctx->nsm, s, P<uint32_t>(ctx->perm), P<uint32_t>(ctx->ptri), kind));
         CK(rfk::launch_items(vjd, nj, P<uint32_t>(ctx->mask), ntiles, P<unsigned long long>(ctx->marks),
                              (uint32_t)ctx->nsm * 16u, P<uint32_t>(ctx->items), counters, s));

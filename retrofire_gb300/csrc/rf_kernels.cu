@@ -657,9 +657,9 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                         const uint32_t *__restrict__ toff, const uint32_t *__restrict__ tpoly,
                         const PolyVert *__restrict__ pool, PrimRec *__restrict__ prims,
                         unsigned long long *__restrict__ rows_total, RasterPrim *__restrict__ rprims,
-                        uint2 *__restrict__ live, uint32_t *__restrict__ live_n,
-                        uint2 *__restrict__ live_small, uint32_t *__restrict__ live_small_n,
-                        uint2 *__restrict__ live_mid, uint32_t *__restrict__ live_mid_n,
+                        uint32_t *__restrict__ live, uint32_t *__restrict__ live_n,
+                        uint32_t *__restrict__ live_small, uint32_t *__restrict__ live_small_n,
+                        uint32_t *__restrict__ live_mid, uint32_t *__restrict__ live_mid_n,
                         uint32_t *__restrict__ extra, StatsDev *__restrict__ stats,
                         const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ptri) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *extra = 0;  // the work list's counter
@@ -833,12 +833,12 @@ k_setup(const DrawDev *__restrict__ draws, uint32_t nd,
                 const uint32_t b = __ballot_sync(0xFFFFFFFFu, keep && list == which);
                 if (!b) continue;
                 uint32_t *cnt_w = which == 0 ? live_n : which == 1 ? live_small_n : live_mid_n;
-                uint2 *list_w = which == 0 ? live : which == 1 ? live_small : live_mid;
+                uint32_t *list_w = which == 0 ? live : which == 1 ? live_small : live_mid;
                 const uint32_t lead = __ffs(b) - 1;
                 uint32_t at = 0;
                 if (lane == lead) at = atomicAdd(cnt_w, (uint32_t)__popc(b));
                 at = __shfl_sync(0xFFFFFFFFu, at, lead);
-                if ((b >> lane) & 1u) list_w[at + __popc(b & ((1u << lane) - 1u))] = make_uint2(dst, gt);
+                if ((b >> lane) & 1u) list_w[at + __popc(b & ((1u << lane) - 1u))] = dst;
             }
             // Write out the records built in this step, one per pass.
             while (bal) {
@@ -1007,7 +1007,7 @@ __device__ __forceinline__ void row_record(float lx, float rx, const float *cv, 
 template <int NCT>
 __global__ void __launch_bounds__(256, 4)
 k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
-      PrimRec *__restrict__ prims, const uint2 *__restrict__ live, uint32_t tile_w,
+      PrimRec *__restrict__ prims, const uint32_t *__restrict__ live, uint32_t tile_w,
       uint32_t *__restrict__ rows, unsigned long long rows_cap, RasterPrim *__restrict__ rprims,
       uint32_t *__restrict__ mask, StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
       unsigned long long *__restrict__ marks) {
@@ -1039,10 +1039,9 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
     uint32_t cur = 0;
     // Live-list entries: this warp's current and next triangle (the one
     // after that is loaded one iteration ahead).
-    // (live entry: the output triangle's index, its input triangle's)
-    uint2 pc = wid < nl ? __ldg(live + wid) : make_uint2(0u, 0u);
-    uint2 pn = wid + nw < nl ? __ldg(live + wid + nw) : make_uint2(0u, 0u);
-    fetch(sbuf[wib][0], pc.x, wid < nl);
+    uint32_t pc = wid < nl ? __ldg(live + wid) : 0u;
+    uint32_t pn = wid + nw < nl ? __ldg(live + wid + nw) : 0u;
+    fetch(sbuf[wib][0], pc, wid < nl);
     RasterPrim *R = &srp[wib];
     float (*T)[RF_TILE_H + 4] = stab[wib];
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -1075,12 +1074,12 @@ k_bin(const DrawDev *__restrict__ draws, const JobDev *__restrict__ jobs,
         }
     };
     for (uint32_t i = wid; i < nl; i += nw) {
-        const uint2 pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : make_uint2(0u, 0u);
+        const uint32_t pnn = i + 2 * nw < nl ? __ldg(live + i + 2 * nw) : 0u;
         __syncwarp();  // the other slot's previous triangle is done
-        fetch(sbuf[wib][cur ^ 1u], pn.x, i + nw < nl);
+        fetch(sbuf[wib][cur ^ 1u], pn, i + nw < nl);
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         __syncwarp();
-        const uint32_t p = pc.x;
+        const uint32_t p = pc;
         pc = pn;
         pn = pnn;
         PrimRec *sP = reinterpret_cast<PrimRec *>(sbuf[wib][cur]);  // fields before `runs` only
@@ -1298,7 +1297,7 @@ static_assert(sizeof(RasterPrim) / 16 <= 8, "a group of eight lanes stores a Ras
 template <int NCT, uint32_t G>
 __global__ void __launch_bounds__(256, 4)
 k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
-            const uint2 *__restrict__ live_small, uint2 *__restrict__ live, uint32_t tile_w,
+            const uint32_t *__restrict__ live_small, uint32_t *__restrict__ live, uint32_t tile_w,
             uint32_t *__restrict__ rows, unsigned long long rows_cap, RasterPrim *__restrict__ rprims, uint32_t *__restrict__ mask,
             StatsDev *__restrict__ stats, uint32_t *__restrict__ counters,
             unsigned long long *__restrict__ marks, uint32_t count_slot) {
@@ -1339,10 +1338,10 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
     for (uint32_t w4 = gid - g; w4 < nl; w4 += ng) {
         const uint32_t i = w4 + g;
         const bool act = i < nl;
-        uint2 e = make_uint2(0u, 0u);
+        uint32_t e = 0;  // the output triangle
         if (act) {
             e = __ldg(live_small + i);
-            const uint4 *src = reinterpret_cast<const uint4 *>(prims + e.x);
+            const uint4 *src = reinterpret_cast<const uint4 *>(prims + e);
             for (uint32_t q = gl; q < RF_PRIM_CORE_BYTES / 16; q += G) sbuf[wib][g][q] = src[q];
         }
         __syncwarp();
@@ -1458,7 +1457,7 @@ k_bin_small(const JobDev *__restrict__ jobs, PrimRec *__restrict__ prims,
             if (gl == 0) R->zmax = zhi;
             __syncwarp(gmask);
             const uint4 *rs = reinterpret_cast<const uint4 *>(R);
-            uint4 *dst = reinterpret_cast<uint4 *>(rprims + e.x);
+            uint4 *dst = reinterpret_cast<uint4 *>(rprims + e);
             if (gl < sizeof(RasterPrim) / 16) dst[gl] = rs[gl];
         }
         __syncwarp();
@@ -1600,7 +1599,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
                          PrimRec *prims, unsigned long long *rows_total, uint32_t *rows,
                          unsigned long long rows_cap,
-                         RasterPrim *rprims, uint32_t *mask, uint2 *live, unsigned long long *marks,
+                         RasterPrim *rprims, uint32_t *mask, uint32_t *live, unsigned long long *marks,
                          StatsDev *stats, uint32_t *counters, int nsm, cudaStream_t s,
                          const uint32_t *perm, const uint32_t *ptri, int kind) {
     cudaError_t e = cudaMemsetAsync(rows_total, 0, 8, s);  // the frame's row-record words
@@ -1613,7 +1612,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
     // a third of the way, those with 9 to 16 rows from two thirds.  (A
     // depth-sorted frame's triangles are single clipped pieces.)
     const size_t live_cap = perm ? (size_t)nt : (size_t)nt * RF_MAX_FAN;
-    uint2 *live_small = live + live_cap, *live_mid = live + 2 * live_cap;
+    uint32_t *live_small = live + live_cap, *live_mid = live + 2 * live_cap;
     k_setup<<<blocks, RF_SETUP_THREADS, 0, s>>>(draws, nd, jobs, nt, cpos, tcnt, toff, tpoly, pool,
                                                 prims, rows_total, rprims, live,
                                                 counters + RF_CNT_LIVE, live_small,

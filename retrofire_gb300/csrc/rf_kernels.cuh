@@ -79,9 +79,8 @@ cudaError_t launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t 
 // then k_bin).  rows holds rows_cap words; rows_total (zeroed here)
 // receives the words the frame asked for, each triangle's records placed
 // by k_setup from it; live (room for three times every output triangle)
-// receives, for each triangle that passes the face-cull test, its index
-// and its input triangle's (the record's tri): the regular ones with at
-// most 8 rows on the target (counters[RF_CNT_LIVE_SMALL]) in its second
+// receives the index of each triangle that passes the face-cull test: the
+// regular ones with at most 8 rows on the target (counters[RF_CNT_LIVE_SMALL]) in its second
 // third, with 9 to 16 rows (counters[RF_CNT_LIVE_MID]) in its last, the
 // rest (counters[RF_CNT_LIVE]) in its first; *marks receives the
 // (triangle, tile) bits set in all.  kind: the shader kind of every draw,
@@ -90,7 +89,7 @@ cudaError_t launch_setup(const DrawDev *draws, uint32_t nd, const JobDev *jobs, 
                          uint32_t tile_w, const float4 *cpos, const uint32_t *tcnt,
                          const uint32_t *toff, const uint32_t *tpoly, const PolyVert *pool,
                          PrimRec *prims, unsigned long long *rows_total, uint32_t *rows,
-                         unsigned long long rows_cap, RasterPrim *rprims, uint32_t *mask, uint2 *live,
+                         unsigned long long rows_cap, RasterPrim *rprims, uint32_t *mask, uint32_t *live,
                          unsigned long long *marks, StatsDev *stats, uint32_t *counters, int nsm,
                          cudaStream_t s, const uint32_t *perm = nullptr, const uint32_t *ptri = nullptr,
                          int kind = RF_K_ANY);

@@ -62,7 +62,7 @@ constexpr size_t OFF_ROWTOT = al(OFF_MASK + (size_t)MAX_TILES * (MASK_WORDS + SU
 constexpr size_t OFF_RPRIMS = al(OFF_ROWTOT + 8);
 constexpr size_t OFF_LIVE =
     al(OFF_RPRIMS + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * sizeof(RasterPrim));
-constexpr size_t OFF_MARKS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 24);
+constexpr size_t OFF_MARKS = al(OFF_LIVE + (size_t)RF_NOALLOC_MAX_TRIS * RF_MAX_FAN * 12);
 constexpr size_t OFF_ITEMS = al(OFF_MARKS + 16);
 constexpr size_t OFF_ROWS = al(OFF_ITEMS + (size_t)MAX_TILES * (RF_SPLIT_K + 1) * 4);
 // The rest of the area holds row records; triangles whose records do not
@@ -233,7 +233,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
     uint32_t *mask = reinterpret_cast<uint32_t *>(base + OFF_MASK);
     unsigned long long *rowtot = reinterpret_cast<unsigned long long *>(base + OFF_ROWTOT);
     RasterPrim *rprims = reinterpret_cast<RasterPrim *>(base + OFF_RPRIMS);
-    uint2 *live = reinterpret_cast<uint2 *>(base + OFF_LIVE);
+    uint32_t *live = reinterpret_cast<uint32_t *>(base + OFF_LIVE);
     unsigned long long *marks = reinterpret_cast<unsigned long long *>(base + OFF_MARKS);
     uint32_t *items = reinterpret_cast<uint32_t *>(base + OFF_ITEMS);
     uint32_t *rows = reinterpret_cast<uint32_t *>(base + OFF_ROWS);
