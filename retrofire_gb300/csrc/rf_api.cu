@@ -124,7 +124,7 @@ struct rf_ctx {
     std::unordered_map<uint64_t, Target> targets;
     // per-frame scratch
     DevBuf draws, jobs, cpos, coc, tcnt, toff, tpoly, pool, prims, mask, scan, counters, stats;
-    DevBuf rowtot, rows, rprims, live, marks, items, jstats;
+    DevBuf rowtot, rows, rprims, live, marks, items, jstats, clipq;
     DevBuf lrec, lmask;  // line pass
     // depth-sorted frames: sorted order, source triangles, per-draw counts,
     // sort scratch, the setup pass's draws / jobs, the raster's unit arrays
@@ -592,6 +592,7 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
     if ((st = ensure(ctx, ctx->tcnt, nt * 4))) return st;
     if ((st = ensure(ctx, ctx->toff, nt * 4))) return st;
     if ((st = ensure(ctx, ctx->tpoly, nt * 4))) return st;
+    if ((st = ensure(ctx, ctx->clipq, nt * 4))) return st;
     const uint32_t pool_cap = (uint32_t)nt;
     if ((st = ensure(ctx, ctx->pool, (size_t)pool_cap * RF_POLY_STORE * sizeof(PolyVert)))) return st;
     if ((st = ensure(ctx, ctx->prims, (size_t)nt * RF_MAX_FAN * sizeof(PrimRec)))) return st;
@@ -669,13 +670,12 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
                               counters, P<unsigned long long>(ctx->marks),
                               ctx->nsm, s));
         CK(mark(RF_STAGE_CLIP));
+        // (each triangle's output slots placed by the clip kernels: no scan)
         CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
-                            P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<uint32_t>(ctx->toff),
-                            P<PolyVert>(ctx->pool),
-                            pool_cap, counters, ctx->nsm, s));
+                            P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<uint32_t>(ctx->clipq),
+                            P<PolyVert>(ctx->pool), pool_cap, counters, ctx->nsm, s,
+                            P<uint32_t>(ctx->toff), true));
         CK(mark(RF_STAGE_SCAN));
-        CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
-                            P<uint32_t>(ctx->scan), counters + RF_CNT_PRIMS, s));
         CK(mark(RF_STAGE_SETUP));
         CK(rfk::launch_setup(dd, ndraws, jd, (uint32_t)nt, TW, P<float4>(ctx->cpos),
                              P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), P<uint32_t>(ctx->tpoly),
@@ -713,7 +713,8 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(mark(RF_STAGE_CLIP));
         CK(rfk::launch_clip(dd, ndraws, (uint32_t)nt, P<float4>(ctx->cpos), P<uint8_t>(ctx->coc),
                             P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->tpoly), P<uint32_t>(ctx->toff),
-                            P<PolyVert>(ctx->pool), pool_cap, counters, ctx->nsm, s));
+                            P<PolyVert>(ctx->pool), pool_cap, counters, ctx->nsm, s,
+                            P<uint32_t>(ctx->toff), false));
         CK(mark(RF_STAGE_SCAN));
         CK(rfk::launch_scan(P<uint32_t>(ctx->tcnt), P<uint32_t>(ctx->toff), (uint32_t)nt,
                             P<uint32_t>(ctx->scan), counters + RF_CNT_PRIMS, s));
@@ -847,9 +848,11 @@ rf_status run_jobs(rf_ctx *ctx, const JobIn *in, uint32_t nin, bool per_job,
         CK(cudaEventRecord(tuned->e1, s));
         tuned->pending = true;
     }
-    // vertex, clip (2), scan (3, or 1 for one block), setup, bin (3: 8- and
-    // 16-lane groups, then warps), work list, raster (+ the stats fold)
-    ctx->kernels += (nt <= RF_SCAN_BLOCK_ITEMS ? 10 : 12) + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
+    // vertex, clip (2), setup, bin (3: 8- and 16-lane groups, then warps),
+    // work list, raster (+ the stats fold; a depth-sorted frame adds the
+    // scan of the fan counts, 3 launches or 1 for one block, and its sort)
+    const uint64_t scan_kernels = sorted ? (nt <= RF_SCAN_BLOCK_ITEMS ? 1 : 3) : 0;
+    ctx->kernels += 9 + scan_kernels + (per_job ? 1 : 0) + (any_cull ? 1 : 0) + sort_kernels;
     if (!ctx->rows_evt_pending) {
         CK(cudaMemcpyAsync(ctx->rows_need_host, ctx->rowtot.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaEventRecord(ctx->rows_evt, s));
@@ -1046,7 +1049,7 @@ rf_status rf_ctx_destroy(rf_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->draws, &ctx->jobs, &ctx->cpos, &ctx->coc, &ctx->tcnt, &ctx->toff,
                       &ctx->tpoly, &ctx->pool, &ctx->prims, &ctx->mask, &ctx->scan,
                       &ctx->counters, &ctx->stats,
-                      &ctx->rowtot, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->marks, &ctx->items, &ctx->jstats, &ctx->lrec, &ctx->lmask,
+                      &ctx->rowtot, &ctx->clipq, &ctx->rows, &ctx->rprims, &ctx->live, &ctx->marks, &ctx->items, &ctx->jstats, &ctx->lrec, &ctx->lmask,
                       &ctx->perm, &ctx->ptri, &ctx->nout, &ctx->dsort, &ctx->vdraws, &ctx->vjobs,
                       &ctx->vtoff, &ctx->vtcnt};
     if (ctx->nout_host) cudaFreeHost(ctx->nout_host);

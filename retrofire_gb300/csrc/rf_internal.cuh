@@ -5,7 +5,10 @@
 //   cpos[v]  float4   clip-space position of every vertex of every draw
 //   coc[v]   u8       outcode (clip.rs:240-242)
 //   tcnt[t]  u32      clipped triangles produced by input triangle t (0..7)
-//   toff[t]  u32      exclusive prefix sum of tcnt = first output prim of t
+//   toff[t]  u32      first output prim of t: t's fan holds prims toff[t] ..
+//                     toff[t] + tcnt[t] (a block taken from a running total
+//                     by k_clip, RF_MAX_FAN long for a clipped t; the
+//                     exclusive prefix sum of tcnt in depth-sorted frames)
 //   tpoly[t] u32      pool slot of t's clipped polygon (clipped tris only)
 //   pool     PolyVert[slot][RF_POLY_STORE] Sutherland-Hodgman output polygons
 //   prim[p]  PrimRec  triangle setup: two ScanlineIter starts (raster.rs:248-302)

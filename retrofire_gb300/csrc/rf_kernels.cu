@@ -72,6 +72,7 @@ __global__ void k_vertex(const DrawDev *__restrict__ draws, uint32_t nd, uint32_
             counters[RF_CNT_LIVE] = 0;
             counters[RF_CNT_LIVE_SMALL] = 0;
             counters[RF_CNT_LIVE_MID] = 0;
+            counters[RF_CNT_PRIMS] = 0;
             counters[RF_CNT_CLIPQ] = 0;
             *marks = 0;
         }
@@ -221,23 +222,27 @@ __device__ int clip_plane(int plane, const CV *in, int nin, CV *out, uint32_t na
 }
 }  // namespace
 
+#define RF_CLIP_THREADS 256u  // k_clip's block
 // Classification (clip.rs:245-267 status): one thread per triangle; the
 // few that cross a plane go to a queue for k_clip_poly, so the clipping
 // loop runs on full warps.
 __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t nt_total,
                        const uint8_t *__restrict__ coc, uint32_t *__restrict__ tcnt,
                        uint32_t *__restrict__ tpoly, uint32_t *__restrict__ queue,
-                       uint32_t *__restrict__ counters) {
-    // Warp-uniform loop (the draw lookup is shared by the warp's lanes).
-    for (uint32_t wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wbase < nt_total;
-         wbase += gridDim.x * blockDim.x) {
-        const uint32_t gt = wbase + (threadIdx.x & 31u);
+                       uint32_t *__restrict__ counters, uint32_t *__restrict__ toff,
+                       uint32_t *__restrict__ prim_total) {
+    // Block-uniform loop (the draw lookup is shared by a warp's lanes, the
+    // output slots are taken once per block).
+    __shared__ uint32_t wslot[2][RF_CLIP_THREADS / 32];
+    uint32_t buf = 0;
+    for (uint32_t bbase = blockIdx.x * blockDim.x; bbase < nt_total; bbase += gridDim.x * blockDim.x) {
+        const uint32_t gt = bbase + threadIdx.x;
         const uint32_t di = warp_upper_index(nd, gt < nt_total ? gt : nt_total - 1,
                                              [&](uint32_t i) { return draws[i].tri_base; });
         bool clipped = false;
+        uint32_t cnt = 0;
         if (gt < nt_total) {
             const DrawDev &d = draws[di];
-            uint32_t cnt = 0;
             if (!d.culled) {  // (a culled draw is a render() call that is not made: no output)
                 const uint32_t t = gt - d.tri_base;
                 uint32_t vi[3];
@@ -267,6 +272,37 @@ __global__ void k_clip(const DrawDev *__restrict__ draws, uint32_t nd, uint32_t 
             if (lane == lead) at = atomicAdd(&counters[RF_CNT_CLIPQ], (uint32_t)__popc(bal));
             at = __shfl_sync(0xFFFFFFFFu, at, lead);
             if (clipped) queue[at + __popc(bal & ((1u << lane) - 1u))] = gt;
+        }
+        if (prim_total) {
+            // The triangle's output slots: one for a visible triangle, a
+            // whole fan's worth (RF_MAX_FAN, of which k_clip_poly fills the
+            // first tcnt) for one that crosses a plane, consecutive over the
+            // block and taken from the frame's running total with one atomic
+            // per block (one per warp contends on the counter in frames of
+            // millions of triangles).
+            const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+            const uint32_t vis = __ballot_sync(0xFFFFFFFFu, cnt != 0u);
+            const uint32_t lt = (1u << lane) - 1u;
+            if (lane == 0) wslot[buf][w] = __popc(vis) + RF_MAX_FAN * __popc(bal);
+            __syncthreads();
+            if (w == 0) {
+                const uint32_t v = lane < RF_CLIP_THREADS / 32 ? wslot[buf][lane] : 0u;
+                uint32_t incl = v;
+#pragma unroll
+                for (uint32_t o = 1; o < RF_CLIP_THREADS / 32; o <<= 1) {
+                    const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= o) incl += x;
+                }
+                const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, RF_CLIP_THREADS / 32 - 1);
+                uint32_t at = 0;
+                if (lane == 0 && total) at = atomicAdd(prim_total, total);
+                at = __shfl_sync(0xFFFFFFFFu, at, 0);
+                if (lane < RF_CLIP_THREADS / 32) wslot[buf][lane] = at + incl - v;
+            }
+            __syncthreads();
+            if (cnt || clipped)
+                toff[gt] = wslot[buf][w] + __popc(vis & lt) + RF_MAX_FAN * __popc(bal & lt);
+            buf ^= 1u;  // (the other buffer next: no third barrier)
         }
     }
 }
@@ -1559,10 +1595,12 @@ cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4
 
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
                         const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, uint32_t *queue,
-                        PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s) {
+                        PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s,
+                        uint32_t *toff, bool place) {
     if (nt == 0) return cudaSuccess;
-    const uint32_t blocks = min((nt + 255) / 256, (uint32_t)nsm * 16);
-    k_clip<<<blocks, 256, 0, s>>>(draws, nd, nt, coc, tcnt, tpoly, queue, counters);
+    uint32_t *prim_total = place ? counters + RF_CNT_PRIMS : nullptr;
+    const uint32_t blocks = min((nt + RF_CLIP_THREADS - 1) / RF_CLIP_THREADS, (uint32_t)nsm * 16);
+    k_clip<<<blocks, RF_CLIP_THREADS, 0, s>>>(draws, nd, nt, coc, tcnt, tpoly, queue, counters, toff, prim_total);
     // The queue's length is known on the device only: a grid for all of it
     // at the worst case, each thread striding over what is there.
     const uint32_t pblocks = min((nt + 15) / 16, (uint32_t)nsm * 8);  // 16 triangles per block

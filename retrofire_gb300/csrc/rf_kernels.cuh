@@ -54,16 +54,25 @@
 #define RF_SCAN_BLOCK_ITEMS 4096u  // values one scan block takes (one launch instead of three)
 
 namespace rfk {
-// counters (optional): POOL, QUEUE, LIVE and CLIPQ zeroed for the kernels after
-// it, and *marks (the binning pass's total of (triangle, tile) bits).
+// counters (optional): POOL, QUEUE, LIVE (all three lists), PRIMS and CLIPQ
+// zeroed for the kernels after it, and *marks (the binning pass's total of
+// (triangle, tile) bits).
 cudaError_t launch_vertex(const DrawDev *draws, uint32_t nd, uint32_t nv, float4 *cpos,
                           uint8_t *coc, uint32_t *counters, unsigned long long *marks,
                           int nsm, cudaStream_t s);
-// queue: room for nt triangle indices (scratch until the scan: the caller
-// passes the scan's output array).
+// Clip status, the clipping of the triangles that cross a plane, and each
+// input triangle's fan count tcnt.  queue: room for nt triangle indices.
+// place: each input triangle's first output slot into toff, taken from a
+// running total (counters[RF_CNT_PRIMS]): one slot for a visible triangle,
+// RF_MAX_FAN for one that is clipped (its fan fills the first tcnt), the
+// triangles' blocks in any order -- every later pass finds a triangle's
+// outputs through toff and tcnt.  Otherwise toff is left to the scan
+// (launch_scan), which packs the outputs in clipped order for the depth
+// sort, and the queue may be the scan's output array.
 cudaError_t launch_clip(const DrawDev *draws, uint32_t nd, uint32_t nt, const float4 *cpos,
                         const uint8_t *coc, uint32_t *tcnt, uint32_t *tpoly, uint32_t *queue,
-                        PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s);
+                        PolyVert *pool, uint32_t pool_cap, uint32_t *counters, int nsm, cudaStream_t s,
+                        uint32_t *toff, bool place);
 // BBox::of a mesh's positions (the first three floats of each vertex of
 // stride floats) into bbox[0..6); bbox[6 ..) is scratch for the per-block
 // parts: bbox holds RF_MESH_BBOX_FLOATS floats.

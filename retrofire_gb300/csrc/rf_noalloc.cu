@@ -251,7 +251,7 @@ extern "C" rf_status rf_render_noalloc(const float *verts, uint32_t nverts, uint
         NA_CK(cudaMemsetAsync(mask, 0, (size_t)ntiles * (J.mask_words + J.sum_words) * 4, s));
         NA_CK(rfk::launch_vertex(dd, 1, nverts, cpos, coc, cnt, marks, nsm, s));
         NA_CK(rfk::launch_clip(dd, 1, ntri, cpos, coc, tcnt, tpoly, toff, pool, RF_NOALLOC_MAX_TRIS,
-                               cnt, nsm, s));
+                               cnt, nsm, s, toff, false));  // (the scan places the outputs)
         NA_CK(rfk::launch_scan(tcnt, toff, ntri, scan, cnt + RF_CNT_PRIMS, s));
         NA_CK(rfk::launch_setup(dd, 1, jd, ntri, TILE_W, cpos, tcnt, toff, tpoly, pool, prims,
                                 rowtot, rows, ROWS_WORDS, rprims, mask, live,

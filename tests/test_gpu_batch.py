@@ -231,9 +231,9 @@ def test_graph_replay_same_shape():
         cnt = dev.counts()
         assert cnt["graphs_cached"] == 1
         assert cnt["graph_launches"] == 6
-        # per frame: ten render kernels (a one-block scan) and the mesh
-        # upload's two bounding-box kernels
-        assert cnt["kernels"] == 6 * (10 + 2)
+        # per frame: nine render kernels and the mesh upload's two
+        # bounding-box kernels
+        assert cnt["kernels"] == 6 * (9 + 2)
     finally:
         dev.close()
 
