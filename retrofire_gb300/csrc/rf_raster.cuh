@@ -923,6 +923,57 @@ __device__ __forceinline__ void tile_rows_coalesced(uint32_t *__restrict__ tile,
     }
 }
 
+// The tile's write-back as bulk copies (cp.async.bulk, the copy engine's
+// untiled form), for tiles of whole 32-column blocks whose rows start
+// 16-byte aligned.  Each 32 x 32 block of the column-major colour tile,
+// then of the depth tile, is transposed into 32 rows of exactly 128 bytes
+// -- lane r writes word x of row r at step k = x - r (mod 32), so both the
+// column reads and the row writes hit 32 different banks -- and lane r
+// hands row r to the copy engine as one 128-byte copy.  The first block
+// goes to the staging area, every later one into the block read just
+// before it (free once read), so no copy is waited for here: the caller
+// waits (bulk_store_drain) before it next writes the tile or the staging
+// area.  Rows without bit r of `want` are not copied.
+template <int TW>
+__device__ __forceinline__ void tile_store_bulk(uint32_t *__restrict__ scol, uint32_t *__restrict__ sdep,
+                                                bool has_depth, uint32_t *__restrict__ stg,
+                                                uint32_t *__restrict__ gcol, uint32_t *__restrict__ gdep,
+                                                uint32_t pitch, uint32_t want, uint32_t lane) {
+    static_assert(TW % 32 == 0, "whole 32-column blocks");
+    constexpr uint32_t NB = (uint32_t)TW / 32u, BW = 32u * RF_TILE_H;  // blocks per buffer, words per block
+    uint32_t *dst = stg;
+#pragma unroll 1
+    for (uint32_t m = 0; m < (has_depth ? 2u * NB : NB); ++m) {
+        const uint32_t bi = m < NB ? m : m - NB;  // block within its buffer
+        uint32_t *src = (m < NB ? scol : sdep) + bi * BW;
+        uint32_t *g = (m < NB ? gcol : gdep) + bi * 32u;
+#pragma unroll 8
+        for (uint32_t k = 0; k < 32; ++k) {
+            const uint32_t x = (lane + k) & 31u;
+            dst[lane * 32 + x] = src[x * RF_TILE_H + lane];
+        }
+        // (rows written through the generic path, read by the copy engine)
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncwarp();
+        if ((want >> lane) & 1u) {
+            const uint32_t sa = (uint32_t)__cvta_generic_to_shared(dst + lane * 32);
+            asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], 128;\n" ::"l"(
+                             g + (size_t)lane * pitch),
+                         "r"(sa)
+                         : "memory");
+        }
+        dst = src;
+    }
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+
+// Every bulk copy this lane issued has read its shared-memory source (the
+// tile and the staging area may be written again once the warp is past it).
+__device__ __forceinline__ void bulk_store_drain() {
+    asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+    __syncwarp();
+}
+
 }  // namespace rfr
 
 // KIND: shader kind of every draw of the job (or RF_K_ANY); FAST: the
@@ -940,6 +991,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
     extern __shared__ __align__(16) uint32_t smem[];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr uint32_t WARP_WORDS = raster_warp_words<TW, KIND>();
+    static_assert(WARP_WORDS % 4u == 0u && (2u * TW * RF_TILE_H) % 4u == 0u,
+                  "each warp's area and its staging start 16-byte aligned (bulk copies)");
     constexpr uint32_t RW = row_words(PreNC<KIND>::NC) * RF_TILE_H;  // words per row slot
     uint32_t *scol = smem + warp * WARP_WORDS;
     float *sdep = reinterpret_cast<float *>(scol + TW * RF_TILE_H);
@@ -964,6 +1017,7 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         if (item == 0xFFFFFFFFu) break;
         const uint32_t tile = item >> RF_ITEM_SHIFT, slice = item & ((1u << RF_ITEM_SHIFT) - 1u);  // 0: the whole tile
         if (tile >= ntiles_total) break;
+        if constexpr (TW % 32 == 0) bulk_store_drain();  // (the last tile's write-back)
         const uint32_t ji = upper_index(nj, tile, [&](uint32_t i) { return jobs[i].tile_base; });
         const JobDev &J = jobs[ji];
         const uint32_t lt = tile - J.tile_base;
@@ -1119,9 +1173,15 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         }
         if (loaded) {
             if (vec) {
-                tile_rows_coalesced<TW, false>(scol, stg, gcol, J.w, rows_ok, lane);
-                if (T.has_depth)
-                    tile_rows_coalesced<TW, false>(reinterpret_cast<uint32_t *>(sdep), stg, gdep, J.w, rows_ok, lane);
+                if constexpr (TW % 32 == 0) {
+                    tile_store_bulk<TW>(scol, reinterpret_cast<uint32_t *>(sdep), T.has_depth, stg, gcol, gdep,
+                                        J.w, rows_ok, lane);
+                } else {
+                    tile_rows_coalesced<TW, false>(scol, stg, gcol, J.w, rows_ok, lane);
+                    if (T.has_depth)
+                        tile_rows_coalesced<TW, false>(reinterpret_cast<uint32_t *>(sdep), stg, gdep, J.w,
+                                                       rows_ok, lane);
+                }
             } else if (T.row_ok) {
                 for (uint32_t x = 0; x < ncols; ++x) {
                     const uint32_t i = x * RF_TILE_H + lane;
@@ -1134,6 +1194,8 @@ k_raster(const JobDev *__restrict__ jobs, uint32_t nj, const DrawDev *__restrict
         const uint32_t j0 = __shfl_sync(0xFFFFFFFFu, ji, 0);
         warp_add_u64(&stats[j0].frags_o, T.frags_o, true);
     }
+    // (shared memory stays allocated until the last write-back has read it)
+    if constexpr (TW % 32 == 0) bulk_store_drain();
 }
 
 namespace rfk {
