@@ -16,10 +16,10 @@ value   fragments (Stats.frags.i) per second with the mesh resident in HBM,
 e2e     the same metric through the C ABI with host buffers: per step the
         mesh is uploaded from pinned host memory, the target cleared and
         rendered, and its colour + depth read back to pinned memory; steps
-        are streamed over two contexts (two CUDA streams, two device meshes
+        are streamed over four contexts (four CUDA streams, two device meshes
         and targets each, async copies on the contexts' copy streams), so
         neighbouring frames and their copies overlap, and timed by the wall
-        clock to the final sync.
+        clock to the final sync over at least 200 frames.
 roofline  achieved = algorithmic bytes of the tile rasteriser per frame
         (4 frags.i + 8 frags.o + 8 W H) / its CUDA-event time; peak = the
         measured HBM copy bandwidth.
@@ -239,13 +239,15 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
     """The metric through the C ABI with host buffers in and out.  Every
     step uploads its mesh from page-locked host memory and reads its colour
     and depth target back into page-locked memory.  Steps are streamed over
-    two contexts (two CUDA streams), each with two device meshes and
+    four contexts (four CUDA streams), each with two device meshes and
     targets: rf_mesh_update_async / rf_target_read_async run on the
-    contexts' copy streams while the other context's frame renders, so one
-    frame's kernels, the next frame's kernels and both frames' copies
-    overlap on the device.  The value is the wall-clock rate up to the final
+    contexts' copy streams while the other contexts' frames render, so
+    neighbouring frames' kernels and copies overlap on the device (1080p
+    fill frame: 267 G frags/s over two contexts, 286 G over three, 290 G
+    over four).  The value is the wall-clock rate up to the final
     sync.  A synchronous step (upload, render, read back, one at a time, one
-    context) gives the latency."""
+    context) gives the latency.  --e2e-contexts sets how many contexts the
+    frames rotate over."""
     import ctypes as C
     import numpy as np
     import torch
@@ -258,13 +260,18 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
         d = torch.empty((H, W), dtype=torch.float32).pin_memory()
         return (c, d, c.numpy().view(np.uint32), d.numpy())
 
-    dev2 = rf.Device()
-    dev2.set_tiling(*dev.last_tiling())  # the tile width the first context settled on
-    dev2.set_graphs(True)  # both contexts replay each frame's launches as one graph
+    nctx = max(1, args.e2e_contexts)
+    extra = []
+    for _ in range(nctx - 1):
+        d = rf.Device()
+        d.set_tiling(*dev.last_tiling())  # the tile width the first context settled on
+        d.set_graphs(True)  # every context replays each frame's launches as one graph
+        extra.append(d)
+    devs = [dev] + extra
     own = []  # the objects created here (closed at the end)
-    slots = []  # (device, mesh, target, pinned outputs): frames alternate devices
+    slots = []  # (device, mesh, target, pinned outputs): frames rotate over the contexts
     for b in range(2):
-        for d in (dev, dev2):
+        for d in devs:
             if d is dev and b == 0:
                 m, t = mesh, tg
             else:
@@ -283,8 +290,8 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
             if i + 1 < n:
                 slots[(i + 1) % len(slots)][1].update_async(vnp, inp)
             t.read_async(o[2], o[3])
-        dev.sync()
-        dev2.sync()
+        for d in devs:
+            d.sync()
 
     def sync_step():
         mesh.update(vnp, inp)
@@ -296,7 +303,7 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
         if code:
             raise rf.RfError(code, "rf_target_read")
 
-    streamed(max(4, args.warmup))
+    streamed(max(len(slots), args.warmup))  # (every slot at least once)
     # every slot renders the same frame: their read-backs agree bit for bit
     ref = None
     for _, _, _, o in slots:
@@ -304,11 +311,14 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
         if ref is not None and h != ref:
             raise RuntimeError("streamed frames differ between contexts")
         ref = h
+    # (at least 200 frames: the wall clock of a few milliseconds of frames
+    # varies by several per cent from run to run)
+    nfr = max(args.steps, 200)
     t0 = time.perf_counter()
-    streamed(args.steps)
+    streamed(nfr)
     wall = time.perf_counter() - t0
-    dev.take_stats()
-    dev2.take_stats()
+    for d in devs:
+        d.take_stats()
     lat = []
     for _ in range(max(3, min(args.steps, 20))):
         t1 = time.perf_counter()
@@ -316,15 +326,16 @@ def run_e2e(args, rf, dev, mesh, tg, sh, ctx, vp, s, frags_i, world):
         lat.append(time.perf_counter() - t1)
     for o in own:
         o.close()
-    dev2.close()
+    for d in extra:
+        d.close()
     lat_ms = sorted(x * 1e3 for x in lat)
     total_ms = max_over_ranks(1e3 * wall, world, "cuda")
-    return {"value": replica_rate(frags_i * args.steps, world, total_ms), "unit": "frags/s",
+    return {"value": replica_rate(frags_i * nfr, world, total_ms), "unit": "frags/s", "frames": nfr,
             "h2d_bytes_per_step": int(s["verts"].nbytes + s["faces"].nbytes),
             "d2h_bytes_per_step": int(2 * 4 * W * H),
-            "mode": "streamed over two contexts (two CUDA streams) with two device meshes and "
+            "mode": "streamed over %d contexts (%d CUDA streams) with two device meshes and "
                     "targets each, async copies on the contexts' copy streams, CUDA graph "
-                    "replay, wall clock to the final sync",
+                    "replay, wall clock to the final sync" % (nctx, nctx),
             "latency_ms": {"p50": lat_ms[len(lat_ms) // 2],
                            "p99": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
                            "note": "one synchronous step on one context: upload, render, "
@@ -891,6 +902,8 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
+    ap.add_argument("--e2e-contexts", type=int, default=4,
+                    help="contexts (CUDA streams) the end-to-end leg streams its frames over")
     ap.add_argument("--no-flush", action="store_true", help="no L2 flush buffer (profiling)")
     ap.add_argument("--workload", default="fill", choices=["fill", "cube", "cubes", "batch", "serve"],
                     help="fill: the headline frame (default); cube: 640x480 textured cube "
