@@ -24,7 +24,9 @@
 // (rfx::jump) of whole tile widths from the boundary values -- then steps
 // pixel by pixel like Iter::next.  Warps take work items (a tile, or a row
 // slice of a crowded one) from the list k_tile_items builds; triangle
-// headers and row records come in through cp.async rings in shared memory.
+// headers and row records come in through cp.async rings in shared memory,
+// and a tile of whole 32-column blocks goes back to HBM through the copy
+// engine (cp.async.bulk, one 128-byte row per lane).
 // ---------------------------------------------------------------------------
 namespace rfr {
 using namespace rfx;
