@@ -186,6 +186,18 @@ def test_tilings_agree(tile):
     assert_parity(g, o, what="tile %r" % (tile,))
 
 
+@pytest.mark.parametrize("tile,depth", [((32, 4), True), ((64, 8), True), ((32, 4), False),
+                                        ((64, 2), False)])
+def test_bulk_write_back(tile, depth):
+    """A target whose rows start 16-byte aligned (width a multiple of 4):
+    its tiles of whole 32-column blocks go back to memory as bulk copies,
+    one 128-byte row per lane, with and without a depth buffer; the edge
+    tiles (520 = 16 x 32 + 8) take the per-pixel path beside them."""
+    draws, vp, w, h = small_fill(seed=13, ntri=3000, w=520, h=300)
+    g, o = both(draws, vp, w, h, tile=tile, depth=depth)
+    assert_parity(g, o, what="tile %r depth %r" % (tile, depth))
+
+
 # ------------------------------------------------------------ edge cases ---
 
 def test_empty_and_degenerate():
